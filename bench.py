@@ -1,0 +1,440 @@
+#!/usr/bin/env python
+"""Throughput of pmwd's particle-mesh hot path on GB300.
+
+One bench step = one forward leapfrog step (K/2 D F K/2, nbody.py:121-140)
+plus one reversible-adjoint step (kick_adj, drift_adj, force_adj, kick_adj,
+nbody.py:143-162) of the 512^3-particle / 1024^3-mesh simulation (box
+1024 Mpc/h, 2LPT initial conditions at a = 1/64, 100 steps to a = 1),
+starting from the 2LPT state.  The metric is particle-steps per second of
+forward + adjoint (N particles per step pair).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl pmx|reference]
+
+N > 1 (torchrun): independent replicas, one per GPU (the path does not
+shard); value = total particle-steps of all ranks / max-over-ranks time.
+``--impl reference`` times the CPU restatement of the reference algorithm
+(the NumPy/SciPy oracle) on the host cores, on a bounded sample.
+"""
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = 'ptcl-steps/s fwd+adjoint at 512^3'
+UNIT = 'ptcl-steps/s'
+
+# Cosmology of the reference's configurations (A_s = 2.1e-9, n_s = 0.965,
+# Omega_m = 0.3, Omega_b = 0.05, h = 0.7).
+COSMO = dict(A_s_1e9=2.1, n_s=0.965, Omega_m=0.3, Omega_b=0.05, h=0.7)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='pmx', choices=['pmx', 'reference'])
+    ap.add_argument('--ptcl', type=int, default=512, help='particle grid side')
+    ap.add_argument('--mesh', type=float, default=2, help='mesh / particle grid ratio')
+    ap.add_argument('--spacing', type=float, default=2.0, help='particle spacing [Mpc/h]')
+    ap.add_argument('--nbody-steps', type=int, default=100)
+    ap.add_argument('--cpu-sample', type=int, default=48,
+                    help='particle grid side of the bounded CPU sample')
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+
+def algorithmic_bytes(N, M, Mc):
+    """Compulsory HBM bytes of every stage, each operand counted once
+    (float32 particle arrays 12 B per particle and array, int16 pmid 6 B,
+    float32 mesh 4 B per cell, complex64 8 B per complex cell)."""
+    return {
+        'fill': None,                       # per launch size differs (M or 3M)
+        'deposit_fwd': 6 * N + 36 * N + 24 * N + 4 * M,
+        'r2c': 4 * M + 8 * Mc,
+        'poisson_fwd': 8 * Mc + 24 * Mc,
+        'c2r_x3': 3 * (8 * Mc + 4 * M),
+        'gather3_kick': 6 * N + 12 * N + 12 * M + 12 * N + 24 * N,
+        'kick_drift_adj_deposit': 6 * N + 72 * N + 48 * N + 4 * M,
+        'gather3_adj': 6 * N + 24 * N + 24 * N + 12 * M + 12 * M,
+        'r2c_x3': 3 * (4 * M + 8 * Mc),
+        'poisson_adj': 24 * Mc + 8 * Mc,
+        'c2r': 8 * Mc + 4 * M,
+        'scatter_adj_kick': 6 * N + 12 * N + 4 * M + 24 * N + 24 * N + 12 * N + 24 * N,
+        'finish': None,
+    }
+
+
+OWN_KERNELS = ('deposit_fwd', 'poisson_fwd', 'gather3_kick', 'kick_drift_adj_deposit',
+               'gather3_adj', 'poisson_adj', 'scatter_adj_kick')
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed
+    region."""
+
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', f'--query-gpu={self.FIELDS}', '--format=csv,noheader,nounits',
+                 '-lms', '200'], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(',')]
+            if len(p) < 9:
+                continue
+            rows.append(p)
+        idx = {r[0] for r in rows}
+        if len(idx) > 1:
+            rows = [r for r in rows if r[0] == str(self.gpu)]
+        if not rows:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['no samples']}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        pw = [num(r[3]) for r in rows if num(r[3]) is not None]
+        thr = (max(pw) * 0.5) if pw else 0
+        loaded = [num(r[1]) for r in rows if num(r[3]) is not None and num(r[3]) >= thr]
+        names = ('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap')
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == 'active'})
+        return {'sm_mhz': statistics.median(loaded or sm), 'sm_max_mhz': num(rows[0][2]),
+                'reasons': reasons, 'samples': len(rows), 'power_w_max': max(pw) if pw else None}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of each stage from the committed ncu summary
+    (profiles/dram_traffic.txt: '<stage> <bytes per launch>' lines)."""
+    p = os.path.join(ROOT, 'profiles', 'dram_traffic.txt')
+    out = {}
+    try:
+        with open(p) as f:
+            for ln in f:
+                ln = ln.strip()
+                if not ln or ln.startswith('#'):
+                    continue
+                k, v = ln.split()[:2]
+                out[k] = float(v)
+    except OSError:
+        pass
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (CPU restatement of the reference algorithm)
+# ---------------------------------------------------------------------------
+
+def cpu_step_pair_rate(side, mesh, spacing, nbody_steps, reps=1):
+    """Particle-steps/s of the oracle for one forward + one adjoint step at a
+    side^3 particle grid (same mesh ratio and spacing)."""
+    import numpy as np
+    from oracle import cosmo as oc, ics, nbody as onb
+    conf = oc.OConf(spacing, (side,) * 3, mesh, float_dtype=np.float32,
+                    a_nbody_maxstep=(1 - 1 / 64) / nbody_steps)
+    cos = oc.with_tables(oc.simple_lcdm(A_s_1e9=COSMO['A_s_1e9'], n_s=COSMO['n_s']), conf)
+    pmid, disp = ics.gen_grid(conf)
+    rng = np.random.default_rng(0)
+    disp = (disp + rng.normal(0, 0.1 * spacing, disp.shape)).astype(np.float32)
+    vel = rng.normal(0, 0.01, disp.shape).astype(np.float32)
+    st = onb.force(conf.a_nbody[0], onb.State(pmid, disp, vel), cos, conf)
+    cot = onb.Cot(rng.normal(size=disp.shape).astype(np.float32),
+                  rng.normal(size=disp.shape).astype(np.float32))
+    a0, a1 = conf.a_nbody[0], conf.a_nbody[1]
+    times = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        st1 = onb.integrate(a0, a1, st, cos, conf)
+        sens = {'factors': [], 'Omega_m': 0.0}
+        st1, cot1, _ = onb.force_adj(a1, st1, cot, cos, conf)
+        onb.integrate_adj(a1, a0, st1, cot1, cos, 0.0, conf, sens)
+        times.append(time.perf_counter() - t)
+    n = conf.ptcl_num
+    return n, times
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    side = args.cpu_sample
+    cores = os.cpu_count()
+    n, times = cpu_step_pair_rate(side, args.mesh, args.spacing, args.nbody_steps,
+                                  reps=args.warmup + args.steps)
+    timed = times[args.warmup:]
+    value = n * len(timed) / sum(timed)
+    sample = (f'NumPy/SciPy oracle (CPU restatement of pmwd; JAX is not installed), one forward '
+              f'+ one adjoint leapfrog step per bench step at {side}^3 particles on a '
+              f'{int(round(side * args.mesh))}^3 mesh (same mesh ratio and spacing as the '
+              f'{args.ptcl}^3 workload); FFTs on {cores} threads, particle work single-threaded')
+    line = {'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT,
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': 1e3 * sum(timed) / len(timed), 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': f'{args.ptcl}^3 ptcl / {int(round(args.ptcl * args.mesh))}^3 '
+                                   f'mesh fwd+adjoint step (sampled at {side}^3)'},
+            'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                             'sample': sample},
+            'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_pmx(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import pmwd_gb300 as pg
+    from pmwd_gb300 import _lib
+    import importlib
+    gnb = importlib.import_module("pmwd_gb300.nbody")
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device('cuda', local_rank)
+    lib = _lib.load()
+
+    side = args.ptcl
+    conf = pg.Configuration(args.spacing, (side,) * 3, args.mesh,
+                            a_nbody_maxstep=(1 - 1 / 64) / args.nbody_steps)
+    cosmo = pg.boltzmann(pg.Cosmology(conf, **COSMO), conf)
+    N, M = conf.ptcl_num, conf.mesh_size
+    Mc = conf.mesh_shape[0] * conf.mesh_shape[1] * (conf.mesh_shape[2] // 2 + 1)
+
+    # 2LPT initial conditions from seeded white noise (one realisation per rank)
+    with torch.no_grad():
+        modes = pg.white_noise(rank, conf, device=dev)
+        modes = pg.linear_modes(modes, cosmo, conf)
+        ptcl, _ = pg.lpt(modes, cosmo, conf)
+        del modes
+    pmid = ptcl.pmid.contiguous()
+    disp = ptcl.disp.contiguous()
+    vel = ptcl.vel.contiguous()
+    acc = torch.empty_like(disp)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1234 + rank)
+    disp_cot = torch.randn(disp.shape, generator=g, device=dev)
+    vel_cot = torch.randn(disp.shape, generator=g, device=dev)
+    alpha = torch.zeros_like(disp)
+    torch.cuda.empty_cache()
+
+    # factors of the first step and of its adjoint (float64 -> float32)
+    fwd = gnb.op_factors(gnb.forward_ops(conf), cosmo, conf).detach()
+    adj = gnb.op_factors(gnb.adjoint_ops(conf), cosmo, conf).detach()
+    f_fwd = (_lib.c_f * 3)(*fwd[:3].to(torch.float32).tolist())
+    f_adj = (_lib.c_f * 3)(*adj[-3:].to(torch.float32).tolist())
+    Om = float(cosmo.Omega_m)
+
+    ws = _lib.workspace(conf.mesh_shape, adjoint=True)
+    spec = _lib.make_spec(3, conf.mesh_shape, conf.mesh_shape, conf.cell_size)
+    dots = torch.zeros(4, dtype=torch.float64, device=dev)
+    P = _lib.ptr
+
+    def step(stream):
+        _lib.check(lib.pmx_nbody_step(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc), N, N,
+                                      f_fwd, Om, stream), 'pmx_nbody_step')
+        _lib.check(lib.pmx_nbody_adj_step(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc),
+                                          P(disp_cot), P(vel_cot), P(alpha), N, N, f_adj, Om,
+                                          P(dots), stream), 'pmx_nbody_adj_step')
+
+    stream = torch.cuda.current_stream(dev)
+    sp = _lib.c_p(stream.cuda_stream)
+    _lib.check(lib.pmx_force(ws.handle, spec, P(pmid), P(disp), N, N, Om, P(acc), sp), 'force')
+    for _ in range(args.warmup):
+        step(sp)
+    torch.cuda.synchronize()
+    _lib.profile_read(ws)  # clear counters
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    lib.pmx_profile_enable(ws.handle, 1)
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step(sp)
+    e1.record(stream)
+    barrier()
+    lib.pmx_profile_enable(ws.handle, 0)
+    clk = clocks.stop()
+    ms_total = e0.elapsed_time(e1)
+    stages, launches = _lib.profile_read(ws)
+    t = torch.tensor([ms_total], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_total = float(t)
+    ms_step = ms_total / args.steps
+    value = world * N * args.steps / (ms_total / 1e3)
+
+    # ---- e2e: the same step pair through the C ABI with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        dev_bufs = dict(pmid=pmid, disp=disp, vel=vel, acc=acc, disp_cot=disp_cot,
+                        vel_cot=vel_cot, alpha=alpha)
+        host = {}
+        for k, v in dev_bufs.items():
+            host[k] = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+            host[k].copy_(v)
+        h2d = sum(v.numel() * v.element_size() for v in host.values())
+        outs = ('disp', 'vel', 'acc', 'disp_cot', 'vel_cot', 'alpha')
+        d2h = sum(host[k].numel() * host[k].element_size() for k in outs)
+        ke = max(2, min(args.steps, 5))
+        barrier()
+        e0.record(stream)
+        for _ in range(ke):
+            for k, v in host.items():
+                dev_bufs[k].copy_(v, non_blocking=True)
+            step(sp)
+            for k in outs:
+                host[k].copy_(dev_bufs[k], non_blocking=True)
+        e1.record(stream)
+        barrier()
+        t = torch.tensor([e0.elapsed_time(e1)], dtype=torch.float64, device=dev)
+        if world > 1:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e = {'value': world * N * ke / (float(t) / 1e3), 'unit': UNIT,
+               'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
+               'steps': ke, 'path': 'pmx_nbody_step + pmx_nbody_adj_step (C ABI), pinned host '
+                                    'buffers copied in and out every step'}
+
+    if rank != 0:
+        return
+
+    # ---- roofline of the dominant own kernel and of the whole step ----
+    peak, peak_kind = measured_peak()
+    ab = algorithmic_bytes(N, M, Mc)
+    traffic = ncu_traffic()
+    stage_rows = {}
+    for name, (ms, calls) in stages.items():
+        if calls == 0:
+            continue
+        per = ms / calls
+        b = ab.get(name)
+        stage_rows[name] = {'ms_per_step': ms / args.steps, 'ms_per_launch': per,
+                            'gbs': (b / (per / 1e3) / 1e9) if b else None}
+    own = {k: v for k, v in stage_rows.items() if k in OWN_KERNELS}
+    dom = max(own, key=lambda k: own[k]['ms_per_step'])
+    ach = stage_rows[dom]['gbs']
+    tr = traffic.get(dom)
+    roofline = {'bound': 'hbm', 'kernel': dom, 'achieved': ach, 'peak': peak, 'unit': 'GB/s',
+                'frac': ach / peak, 'traffic': tr,
+                'algorithmic_bytes': ab[dom], 'peak_kind': f'{peak_kind} (MEASURED_PEAKS.json hbm_gbs)'
+                if peak_kind == 'measured' else 'fallback 6.8 TB/s'}
+    step_bytes = 492 * N + 204 * M
+    step_gbs = step_bytes / (ms_step / 1e3) / 1e9
+
+    cpu = None
+    if not args.no_cpu:
+        cs = args.cpu_sample
+        n_cpu, times = cpu_step_pair_rate(cs, args.mesh, args.spacing, args.nbody_steps, reps=1)
+        cpu = {'value': n_cpu / times[0], 'unit': UNIT, 'cores': os.cpu_count(), 'kind': 'port',
+               'sample': f'one fwd+adj step pair of the NumPy/SciPy oracle at {cs}^3 particles / '
+                         f'{int(round(cs * args.mesh))}^3 mesh ({times[0]:.1f} s); FFTs on all '
+                         f'cores, particle work single-threaded'}
+
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms_step, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic: seeded white noise -> E&H linear power -> 2LPT at a=1/64',
+        'config': {'workload': f'{side}^3 ptcl / {conf.mesh_shape[0]}^3 mesh, box '
+                               f'{side * args.spacing:g} Mpc/h, 1 fwd + 1 adjoint leapfrog step '
+                               f'of a {args.nbody_steps}-step run',
+                   'ptcl': N, 'mesh_cells': M, 'parallelism': f'replicas x{world}',
+                   'l2': 'inputs larger than L2 (mesh 4.3 GB per array)'},
+        'roofline': roofline,
+        'step_roofline': {'bytes_per_step': step_bytes, 'achieved': step_gbs, 'peak': peak,
+                          'frac': step_gbs / peak, 'unit': 'GB/s',
+                          'convention': '492 N + 204 M bytes per fwd+adj step pair'},
+        'stages': stage_rows,
+        'cpu_baseline': cpu,
+        'e2e': e2e,
+        'gpu_launches': launches,
+        'clocks': clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get('RANK', 0))
+    world = int(os.environ.get('WORLD_SIZE', 1))
+    local_rank = int(os.environ.get('LOCAL_RANK', 0))
+    if args.impl == 'reference':
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group('nccl')
+    run_pmx(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

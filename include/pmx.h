@@ -1,0 +1,220 @@
+/*
+ * pmx.h -- C ABI of the GB300 particle-mesh library (libpmx.so).
+ *
+ * Replaces the compute underneath pmwd's Python operators; each entry point
+ * names the reference function (path:line inside the pmwd project) whose
+ * behaviour it reproduces.  Conventions:
+ *
+ *  - All array arguments are caller-owned DEVICE pointers, row-major:
+ *    pmid int16 (n, dim), disp/vel/acc/cotangents float32 (n, dim),
+ *    meshes float32 (mesh_shape..., channels).
+ *  - Every call is asynchronous on the given CUDA stream (cudaStream_t passed
+ *    as void*; NULL = legacy default stream) and never synchronises the host.
+ *  - Every call returns PMX_OK (0) or a negative status; pmx_last_error()
+ *    returns a thread-local message describing the last failure.
+ *  - No C++ exception crosses this boundary.  Re-entrant: calls on different
+ *    workspaces / streams may run concurrently.
+ */
+#ifndef PMX_H
+#define PMX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PMX_OK          0
+#define PMX_ERR_ARG    -1   /* bad argument value or null pointer          */
+#define PMX_ERR_SHAPE  -2   /* inconsistent shapes                         */
+#define PMX_ERR_ALIGN  -3   /* pointer alignment requirement violated      */
+#define PMX_ERR_CUDA   -4   /* CUDA runtime error                          */
+#define PMX_ERR_CUFFT  -5   /* cuFFT error                                 */
+#define PMX_ERR_NOMEM  -6   /* device allocation failed                    */
+
+/* Geometry of one enmesh (pm_util.py:33-156 ``enmesh``) as scatter/gather
+ * call it: grid 1 is the particle grid of conf (cell size a1 =
+ * conf.cell_size, periodic shape s1 = conf.mesh_shape); grid 2 is the target
+ * mesh with spatial shape mesh_shape, origin offset b12 and cell size a2
+ * (cell_size <= 0 means the reference's ``cell_size=None``). */
+typedef struct pmx_enmesh_spec {
+    int32_t dim;             /* spatial dimension, 1..3                    */
+    int32_t wrap_shape[3];   /* conf.mesh_shape (s1), first `dim` used     */
+    int64_t mesh_shape[3];   /* spatial shape of the mesh array (s2)       */
+    double  conf_cell_size;  /* conf.cell_size (a1)                        */
+    double  offset[3];       /* offset of mesh to particle grid (b12)      */
+    double  cell_size;       /* mesh cell size a2, <= 0 for None           */
+} pmx_enmesh_spec;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int pmx_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *pmx_last_error(void);
+
+/* Number of SMs of the current device, used to size persistent grids. */
+int pmx_device_sms(int *sms);
+
+/* --------------------------------------------------------------------------
+ * Mesh operators
+ * ------------------------------------------------------------------------ */
+
+/* Multilinear indices, fractions and fraction gradients of every particle,
+ * pmwd/particles.py:212-254 ``ptcl_enmesh`` -> pm_util.py:33-156.
+ * ind (n, 2^dim, dim) int32, frac (n, 2^dim), frac_grad (n, 2^dim, dim);
+ * ind and frac_grad may be NULL.  Indices are bit-exact with the reference
+ * (wrapped by s1, never dropped). */
+int pmx_enmesh(const pmx_enmesh_spec *spec, const int16_t *pmid,
+               const float *disp, int64_t n, int32_t *ind, float *frac,
+               float *frac_grad, void *stream);
+
+/* mesh[i_k, c] += val[p, c] * frac_k for the 2^dim neighbours of each
+ * particle, out-of-range neighbours dropped; pmwd/scatter.py:8-83.
+ * val == NULL uses val_scalar for every particle (channels must be 1).
+ * mesh is accumulated in place (the caller zeroes it for a fresh scatter). */
+int pmx_scatter(const pmx_enmesh_spec *spec, const int16_t *pmid,
+                const float *disp, int64_t n, const float *val,
+                float val_scalar, int64_t channels, float *mesh, void *stream);
+
+/* Scatter VJP, pmwd/scatter.py:86-148 (``_scatter_chunk_adj``):
+ * disp_cot (n, dim) = sum_k (mesh_cot[i_k] . val) dfrac_k / cell  (overwritten),
+ * val_cot  (n, channels) = sum_k mesh_cot[i_k] frac_k  (overwritten, may be NULL).
+ * The mesh cotangent passes through unchanged (the caller keeps it). */
+int pmx_scatter_adj(const pmx_enmesh_spec *spec, const int16_t *pmid,
+                    const float *disp, int64_t n, const float *val,
+                    float val_scalar, int64_t channels, const float *mesh_cot,
+                    float *disp_cot, float *val_cot, void *stream);
+
+/* out[p, c] = val[p, c] + sum_k mesh[i_k, c] frac_k, out-of-range neighbours
+ * read as 0; pmwd/gather.py:8-77.  val == NULL uses val_scalar. */
+int pmx_gather(const pmx_enmesh_spec *spec, const int16_t *pmid,
+               const float *disp, int64_t n, const float *mesh,
+               int64_t channels, const float *val, float val_scalar,
+               float *out, void *stream);
+
+/* Gather VJP, pmwd/gather.py:80-144 (``_gather_chunk_adj``):
+ * disp_cot (n, dim) = sum_k (val_cot . mesh[i_k]) dfrac_k / cell (overwritten),
+ * mesh_cot[i_k, c] += val_cot[p, c] frac_k (accumulated; caller zeroes it).
+ * The value cotangent passes through unchanged. */
+int pmx_gather_adj(const pmx_enmesh_spec *spec, const int16_t *pmid,
+                   const float *disp, int64_t n, const float *mesh,
+                   int64_t channels, const float *val_cot, float *disp_cot,
+                   float *mesh_cot, void *stream);
+
+/* --------------------------------------------------------------------------
+ * Poisson force (pmwd/gravity.py:47-72) on a persistent workspace
+ * ------------------------------------------------------------------------ */
+
+typedef struct pmx_workspace pmx_workspace;
+
+#define PMX_WS_ADJOINT 1   /* also allocate buffers for the force VJP */
+
+/* Device bytes a workspace for this 3-D mesh allocates (meshes, spectra,
+ * cuFFT work areas, reduction scratch). */
+int pmx_workspace_bytes(const int64_t mesh_shape[3], int32_t flags,
+                        size_t *bytes);
+
+/* Creates the workspace on the current device: mesh and spectrum buffers,
+ * cuFFT plans (r2c, batched c2r, and for PMX_WS_ADJOINT batched r2c and
+ * c2r) with caller-visible work areas.  This is the only call that
+ * allocates device memory. */
+int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
+                         pmx_workspace **ws);
+int pmx_workspace_destroy(pmx_workspace *ws);
+
+/* Particle accelerations acc (n, 3), pmwd/gravity.py:47-72: CIC density of
+ * mean 1 (val = mesh_size/ptcl_num), overdensity times 1.5*Omega_m, r2c,
+ * -1/k^2 (k=0 -> 0), -i k per axis with the Nyquist plane zeroed, c2r with
+ * 1/N, CIC gather.  No CIC deconvolution (pmwd applies none).  The spec
+ * must be the default enmesh (offset 0, cell_size None), dim 3, and its
+ * mesh_shape equal to the workspace's. */
+int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+              const int16_t *pmid, const float *disp, int64_t n,
+              int64_t ptcl_num, double omega_m, float *acc, void *stream);
+
+/* Forward force plus its VJP against acc_cot (n, 3): the
+ * ``vjp(gravity, ...)`` of pmwd/nbody.py:108-118.  Writes acc (n, 3),
+ * disp_cot (n, 3) and, if omega_m_cot != NULL, the Omega_m cotangent as one
+ * double in DEVICE memory.  Needs a PMX_WS_ADJOINT workspace. */
+int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                  const int16_t *pmid, const float *disp, int64_t n,
+                  int64_t ptcl_num, double omega_m, const float *acc_cot,
+                  float *acc, float *disp_cot, double *omega_m_cot,
+                  void *stream);
+
+/* --------------------------------------------------------------------------
+ * Leapfrog (pmwd/nbody.py) -- all factors are the float32 casts of the
+ * float64 time-step factors the host computes.
+ * ------------------------------------------------------------------------ */
+
+/* vel += acc * factor over n3 = 3*n floats, nbody.py:70-77 ``kick``. */
+int pmx_kick(float *vel, const float *acc, int64_t n3, float factor,
+             void *stream);
+
+/* disp += vel * factor, nbody.py:39-46 ``drift``. */
+int pmx_drift(float *disp, const float *vel, int64_t n3, float factor,
+              void *stream);
+
+/* nbody.py:80-99 ``kick_adj``: vel += acc*K; disp_cot -= acc_cot*K;
+ * dot = sum(vel_cot * acc) written as one double to DEVICE memory (may be
+ * NULL).  The sum is deterministic (fixed two-level order). */
+int pmx_kick_adj(float *vel, const float *acc, float *disp_cot,
+                 const float *acc_cot, const float *vel_cot, int64_t n3,
+                 float factor, double *dot, void *stream);
+
+/* nbody.py:49-67 ``drift_adj``: disp += vel*D; vel_cot -= disp_cot*D;
+ * dot = sum(disp_cot * vel) (DEVICE double, may be NULL). */
+int pmx_drift_adj(float *disp, const float *vel, float *vel_cot,
+                  const float *disp_cot, int64_t n3, float factor,
+                  double *dot, void *stream);
+
+/* Deterministic float64-accumulated dot product of two float32 arrays;
+ * the ``(x * y).sum()`` reductions of nbody.py:67,97. */
+int pmx_dot(const float *x, const float *y, int64_t n, double *out,
+            void *stream);
+
+/* One forward step K(1/2) D F K(1/2) of nbody.py:121-140 (``integrate``
+ * with the default symp_splits), fused: factors = {K1, D, K2}. */
+int pmx_nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                   const int16_t *pmid, float *disp, float *vel, float *acc,
+                   int64_t n, int64_t ptcl_num, const float factors[3],
+                   double omega_m, void *stream);
+
+/* One reverse step of nbody.py:143-162 (``integrate_adj``): kick_adj(K1),
+ * drift_adj(D), force_adj, kick_adj(K2), fused.  acc_cot is pmwd's alpha
+ * (``ptcl_cot.acc``).  dots (DEVICE, 4 doubles) receives
+ * {sum(vel_cot*acc) at K1, sum(disp_cot*vel) at D, sum(vel_cot*acc_new) at
+ * the force and K2, Omega_m cotangent of the new force}. */
+int pmx_nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                       const int16_t *pmid, float *disp, float *vel,
+                       float *acc, float *disp_cot, float *vel_cot,
+                       float *acc_cot, int64_t n, int64_t ptcl_num,
+                       const float factors[3], double omega_m, double *dots,
+                       void *stream);
+
+/* --------------------------------------------------------------------------
+ * Stage profiler (no counterpart in pmwd, which only times whole jitted
+ * calls with timeit): CUDA events around each stage of the force and step
+ * entry points of one workspace.
+ * ------------------------------------------------------------------------ */
+
+#define PMX_PROF_STAGES 13
+
+/* Starts (on != 0) or stops recording stage events on this workspace. */
+int pmx_profile_enable(pmx_workspace *ws, int on);
+
+/* Waits for the recorded events, writes per stage the summed milliseconds
+ * and number of executions (arrays of PMX_PROF_STAGES), and the number of
+ * libpmx kernel launches since the last read (cuFFT's own kernels are not
+ * counted); then clears the records.  Any pointer may be NULL. */
+int pmx_profile_read(pmx_workspace *ws, double *ms, int64_t *calls, int64_t *launches);
+
+/* Name of stage i, or NULL when out of range. */
+const char *pmx_profile_stage_name(int i);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PMX_H */

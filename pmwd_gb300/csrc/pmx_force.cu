@@ -1,0 +1,1141 @@
+// Poisson force, leapfrog and reversible-adjoint kernels (the hot path).
+//
+// Reference: pmwd/gravity.py:47-72 (gravity), pmwd/nbody.py:39-162
+// (drift/kick/force, their adjoints and the symplectic step).  All kernels
+// here are specialised for the path the N-body loop takes: 3-D, default
+// enmesh branch (offset 0, cell_size None), one channel, scalar value
+// conf.mesh_size / conf.ptcl_num.
+//
+// Device layout of a workspace (float32 unless noted):
+//   dens  M           CIC density (initialised to -1, so it holds the overdensity)
+//   ck    3 * Mc      complex64 half spectra (r2c output; the Fourier kernel
+//                     writes the three gradient spectra over it)
+//   g     3 * M       real acceleration meshes (planar, one per axis)
+//   mcot  3 * M       cotangents of g (adjoint workspaces only)
+//   ktab  2*(n0+n1+n2h) angular wavenumbers, plain and Nyquist-masked
+//   part  4 * PMAX    float64 per-block partial sums of the dot products
+// with M = n0*n1*n2 and Mc = n0*n1*(n2/2+1).
+
+#include <cufft.h>
+
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "pmx_internal.cuh"
+
+using namespace pmx;
+
+namespace {
+
+constexpr int PMAX = 4096;       // max blocks of a particle kernel (partials per slot)
+constexpr int NSLOT = 4;         // dot-product slots
+constexpr int PT = 256;          // threads per particle kernel
+constexpr double PI = 3.141592653589793;
+
+const char *cufft_name(cufftResult r) {
+    switch (r) {
+        case CUFFT_SUCCESS: return "CUFFT_SUCCESS";
+        case CUFFT_INVALID_PLAN: return "CUFFT_INVALID_PLAN";
+        case CUFFT_ALLOC_FAILED: return "CUFFT_ALLOC_FAILED";
+        case CUFFT_INVALID_VALUE: return "CUFFT_INVALID_VALUE";
+        case CUFFT_INTERNAL_ERROR: return "CUFFT_INTERNAL_ERROR";
+        case CUFFT_EXEC_FAILED: return "CUFFT_EXEC_FAILED";
+        case CUFFT_SETUP_FAILED: return "CUFFT_SETUP_FAILED";
+        case CUFFT_INVALID_SIZE: return "CUFFT_INVALID_SIZE";
+        default: return "cuFFT error";
+    }
+}
+
+#define PMX_CUFFT(call)                                                                   \
+    do {                                                                                  \
+        cufftResult r_ = (call);                                                          \
+        if (r_ != CUFFT_SUCCESS)                                                          \
+            return fail(PMX_ERR_CUFFT, std::string(#call) + ": " + cufft_name(r_));       \
+    } while (0)
+
+}  // namespace
+
+struct pmx_workspace {
+    int dev = 0;
+    int flags = 0;
+    int64_t n0 = 0, n1 = 0, n2 = 0, n2h = 0, M = 0, Mc = 0;
+    float *dens = nullptr;
+    float2 *ck = nullptr;
+    float *g = nullptr;
+    float *mcot = nullptr;
+    float *ktab = nullptr;
+    double *part = nullptr;
+    void *fft_work = nullptr;
+    size_t fft_work_bytes = 0;
+    cufftHandle r2c1 = 0, c2r3 = 0, r2c3 = 0, c2r1 = 0;
+    bool have_r2c1 = false, have_c2r3 = false, have_r2c3 = false, have_c2r1 = false;
+    double ktab_cell = -1.0;
+    // stage profiler: CUDA events around every stage while enabled
+    bool prof_on = false;
+    struct Rec {
+        int stage;
+        cudaEvent_t b, e;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    int64_t launches = 0;  // launches of libpmx kernels (cuFFT's not counted)
+};
+
+namespace {
+
+const char *const kStageNames[PMX_PROF_STAGES] = {
+    "fill", "deposit_fwd", "r2c", "poisson_fwd", "c2r_x3", "gather3_kick",
+    "kick_drift_adj_deposit", "gather3_adj", "r2c_x3", "poisson_adj", "c2r", "scatter_adj_kick",
+    "finish"};
+
+cudaEvent_t prof_event(pmx_workspace *ws) {
+    if (!ws->pool.empty()) {
+        cudaEvent_t e = ws->pool.back();
+        ws->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+// Brackets one stage with events when profiling is on; counts libpmx
+// kernel launches (nk per stage) always.
+struct Stage {
+    pmx_workspace *ws;
+    int id;
+    cudaStream_t s;
+    cudaEvent_t b = nullptr;
+    Stage(pmx_workspace *w, int stage, cudaStream_t st, int nk) : ws(w), id(stage), s(st) {
+        ws->launches += nk;
+        if (ws->prof_on && (b = prof_event(ws))) cudaEventRecord(b, s);
+    }
+    ~Stage() {
+        if (!b) return;
+        cudaEvent_t e = prof_event(ws);
+        if (!e) {
+            ws->pool.push_back(b);
+            return;
+        }
+        cudaEventRecord(e, s);
+        ws->recs.push_back({id, b, e});
+    }
+};
+
+}  // namespace
+
+namespace pmx {
+
+// ---------------------------------------------------------------------------
+// small kernels
+// ---------------------------------------------------------------------------
+
+__global__ void k_fill(float *p, float v, int64_t n) {
+    int64_t n4 = n >> 2;
+    float4 v4 = make_float4(v, v, v, v);
+    float4 *p4 = reinterpret_cast<float4 *>(p);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4;
+         i += (int64_t)gridDim.x * blockDim.x)
+        p4[i] = v4;
+    for (int64_t i = (n4 << 2) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// Angular wavenumbers of pm_util.py:159-199 (fftfreq * 2*pi/spacing in
+// float64, cast to float32), plain and with the Nyquist entries zeroed as
+// neg_grad does (gravity.py:37-44).
+__global__ void k_ktab(float *kt, int n0, int n1, int n2, double period, float nyq, float eps) {
+    int n2h = n2 / 2 + 1;
+    int tot = n0 + n1 + n2h;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += gridDim.x * blockDim.x) {
+        int n, i;
+        long fi;
+        if (t < n0) {
+            n = n0; i = t; fi = i < (n + 1) / 2 ? i : i - n;
+        } else if (t < n0 + n1) {
+            n = n1; i = t - n0; fi = i < (n + 1) / 2 ? i : i - n;
+        } else {
+            n = n2; i = t - n0 - n1; fi = i;  // rfftfreq
+        }
+        double f = __ddiv_rn((double)fi, (double)n);
+        float k = (float)__dmul_rn(f, period);
+        kt[t] = k;
+        float dk = fabsf(__fsub_rn(fabsf(k), nyq));
+        kt[tot + t] = dk <= eps ? 0.f : k;
+    }
+}
+
+// Forward Fourier kernel, fused laplace + neg_grad for the three axes
+// (gravity.py:9-16, 37-44, 58-62): reads the r2c spectrum of the overdensity
+// and writes -i k_j * (-(F c)/k^2) for j = 0,1,2 (k = 0 -> 0), c = 1.5
+// Omega_m / N folding in the real-space scale and irfftn's 1/N.
+// One warp per (i, j) row of n2h complex values.
+__global__ void k_poisson_fwd(float2 *ck, int64_t n0, int64_t n1, int64_t n2h, int64_t Mc,
+                              const float *__restrict__ kt, float c) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const float *kx = kt, *ky = kt + n0, *kz = kt + n0 + n1;
+    const int64_t tot = n0 + n1 + n2h;
+    const float *mx = kt + tot, *my = kt + tot + n0, *mz = kt + tot + n0 + n1;
+    for (int64_t row = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+         row < n0 * n1; row += warps) {
+        int64_t i = row / n1, j = row - i * n1;
+        float kxi = __ldg(kx + i), kyj = __ldg(ky + j);
+        float mxi = __ldg(mx + i), myj = __ldg(my + j);
+        float kxy = __fadd_rn(__fmul_rn(kxi, kxi), __fmul_rn(kyj, kyj));
+        float2 *r0 = ck + row * n2h;
+        for (int64_t l = lane; l < n2h; l += 32) {
+            float kzl = __ldg(kz + l), mzl = __ldg(mz + l);
+            float k2 = __fadd_rn(kxy, __fmul_rn(kzl, kzl));
+            float2 F = r0[l];
+            float pr = 0.f, pi = 0.f;
+            if (k2 != 0.f) {
+                pr = -__fdiv_rn(__fmul_rn(F.x, c), k2);
+                pi = -__fdiv_rn(__fmul_rn(F.y, c), k2);
+            }
+            // (-i k)(pr + i pi) = (k pi, -k pr)
+            r0[l] = make_float2(__fmul_rn(mxi, pi), -__fmul_rn(mxi, pr));
+            r0[Mc + l] = make_float2(__fmul_rn(myj, pi), -__fmul_rn(myj, pr));
+            r0[2 * Mc + l] = make_float2(__fmul_rn(mzl, pi), -__fmul_rn(mzl, pr));
+        }
+    }
+}
+
+// Adjoint Fourier kernel: the real transpose of the forward operator
+// irfftn o (-i k_j)(-1/k^2) o rfftn is irfftn o (+i k_j)(-1/k^2) o rfftn;
+// summed over the three axes: S = -(c/k^2) sum_j i k_j G_j, written over
+// the first spectrum.
+__global__ void k_poisson_adj(float2 *ck, int64_t n0, int64_t n1, int64_t n2h, int64_t Mc,
+                              const float *__restrict__ kt, float c) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const float *kx = kt, *ky = kt + n0, *kz = kt + n0 + n1;
+    const int64_t tot = n0 + n1 + n2h;
+    const float *mx = kt + tot, *my = kt + tot + n0, *mz = kt + tot + n0 + n1;
+    for (int64_t row = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+         row < n0 * n1; row += warps) {
+        int64_t i = row / n1, j = row - i * n1;
+        float kxi = __ldg(kx + i), kyj = __ldg(ky + j);
+        float mxi = __ldg(mx + i), myj = __ldg(my + j);
+        float kxy = __fadd_rn(__fmul_rn(kxi, kxi), __fmul_rn(kyj, kyj));
+        float2 *r0 = ck + row * n2h;
+        for (int64_t l = lane; l < n2h; l += 32) {
+            float kzl = __ldg(kz + l), mzl = __ldg(mz + l);
+            float k2 = __fadd_rn(kxy, __fmul_rn(kzl, kzl));
+            float2 G0 = r0[l], G1 = r0[Mc + l], G2 = r0[2 * Mc + l];
+            // i k (a + i b) = (-k b, k a)
+            float re = -__fadd_rn(__fadd_rn(__fmul_rn(mxi, G0.y), __fmul_rn(myj, G1.y)),
+                                  __fmul_rn(mzl, G2.y));
+            float im = __fadd_rn(__fadd_rn(__fmul_rn(mxi, G0.x), __fmul_rn(myj, G1.x)),
+                                 __fmul_rn(mzl, G2.x));
+            float sr = 0.f, si = 0.f;
+            if (k2 != 0.f) {
+                sr = -__fdiv_rn(__fmul_rn(re, c), k2);
+                si = -__fdiv_rn(__fmul_rn(im, c), k2);
+            }
+            r0[l] = make_float2(sr, si);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// particle kernels of the hot path (3-D, default enmesh branch)
+// ---------------------------------------------------------------------------
+
+struct Hot {
+    int wrap[3];
+    int64_t stride[3];
+    float cell;   // f32(conf.cell_size), also the disp_cot divisor
+    float val;    // f32(mesh_size / ptcl_num)
+};
+
+__device__ __forceinline__ void hot_axis(const Hot &h, int a, int pm, float d, Axis &ax) {
+    float x = __fdiv_rn(d, h.cell);
+    int fl = (int)floorf(x);
+#pragma unroll
+    for (int nb = 0; nb < 2; ++nb) {
+        int ii = fl + nb;
+        float d2 = __fsub_rn(x, (float)ii);
+        ax.w[nb] = __fsub_rn(1.f, fabsf(d2));
+        ax.s[nb] = sgnf(-d2);
+        ax.i[nb] = pymod(ii + pm, h.wrap[a]);
+    }
+}
+
+__device__ __forceinline__ int64_t hot_cell(const Hot &h, const Axis ax[3], int k) {
+    return (int64_t)ax[0].i[k & 1] * h.stride[0] + (int64_t)ax[1].i[(k >> 1) & 1] * h.stride[1] +
+           (int64_t)ax[2].i[(k >> 2) & 1];
+}
+
+__device__ __forceinline__ float3 ld3(const float *p, int64_t q) {
+    return make_float3(p[3 * q], p[3 * q + 1], p[3 * q + 2]);
+}
+__device__ __forceinline__ void st3(float *p, int64_t q, float3 v) {
+    p[3 * q] = v.x;
+    p[3 * q + 1] = v.y;
+    p[3 * q + 2] = v.z;
+}
+__device__ __forceinline__ float3 axpy3(float3 y, float3 x, float a) {  // y + x*a, unfused
+    return make_float3(__fadd_rn(y.x, __fmul_rn(x.x, a)), __fadd_rn(y.y, __fmul_rn(x.y, a)),
+                       __fadd_rn(y.z, __fmul_rn(x.z, a)));
+}
+__device__ __forceinline__ float3 axmy3(float3 y, float3 x, float a) {  // y - x*a, unfused
+    return make_float3(__fsub_rn(y.x, __fmul_rn(x.x, a)), __fsub_rn(y.y, __fmul_rn(x.y, a)),
+                       __fsub_rn(y.z, __fmul_rn(x.z, a)));
+}
+__device__ __forceinline__ double dot3d(float3 a, float3 b) {
+    return (double)a.x * (double)b.x + (double)a.y * (double)b.y + (double)a.z * (double)b.z;
+}
+
+__device__ __forceinline__ void hot_enmesh(const Hot &h, const int16_t *pmid, int64_t q, float3 d,
+                                           Axis ax[3]) {
+    hot_axis(h, 0, pmid[3 * q], d.x, ax[0]);
+    hot_axis(h, 1, pmid[3 * q + 1], d.y, ax[1]);
+    hot_axis(h, 2, pmid[3 * q + 2], d.z, ax[2]);
+}
+
+__device__ __forceinline__ void hot_deposit(const Hot &h, const Axis ax[3], float *dens) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        atomicAdd(dens + hot_cell(h, ax, k), __fmul_rn(h.val, frac_of(ax, k)));
+}
+
+// Forward: optional kick (vel += acc*K1) and drift (disp += vel*D), then the
+// CIC density deposit of the (new) positions.
+template <bool KD>
+__global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ pmid, float *disp,
+                                            float *vel, const float *__restrict__ acc, int64_t n,
+                                            float K1, float D, float *dens) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        float3 d = ld3(disp, q);
+        if (KD) {
+            float3 v = axpy3(ld3(vel, q), ld3(acc, q), K1);
+            d = axpy3(d, v, D);
+            st3(vel, q, v);
+            st3(disp, q, d);
+        }
+        Axis ax[3];
+        hot_enmesh(h, pmid, q, d, ax);
+        hot_deposit(h, ax, dens);
+    }
+}
+
+// Forward: gather the three acceleration meshes, optionally kick with K2.
+template <bool KICK>
+__global__ void __launch_bounds__(PT) k_gather3(Hot h, const int16_t *__restrict__ pmid,
+                                                const float *__restrict__ disp, float *vel,
+                                                float *acc, int64_t n, int64_t M,
+                                                const float *__restrict__ g, float K2) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        Axis ax[3];
+        hot_enmesh(h, pmid, q, ld3(disp, q), ax);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            int64_t c = hot_cell(h, ax, k);
+            float f = frac_of(ax, k);
+            a0 = __fadd_rn(a0, __fmul_rn(__ldg(g + c), f));
+            a1 = __fadd_rn(a1, __fmul_rn(__ldg(g + M + c), f));
+            a2 = __fadd_rn(a2, __fmul_rn(__ldg(g + 2 * M + c), f));
+        }
+        float3 a = make_float3(a0, a1, a2);
+        st3(acc, q, a);
+        if (KICK) st3(vel, q, axpy3(ld3(vel, q), a, K2));
+    }
+}
+
+// Adjoint: kick_adj(K1) then drift_adj(D) (nbody.py:80-99, 49-67), then the
+// density deposit of the reconstructed positions.  Partial dots:
+// slot 0 = sum(vel_cot*acc), slot 1 = sum(disp_cot*vel).
+template <bool KD>
+__global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pmid, float *disp,
+                                           float *vel, const float *__restrict__ acc,
+                                           float *disp_cot, float *vel_cot,
+                                           const float *__restrict__ alpha, int64_t n, float K1,
+                                           float D, float *dens, double *part) {
+    __shared__ double sh[PT / 32];
+    double s0 = 0.0, s1 = 0.0;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        float3 d = ld3(disp, q);
+        if (KD) {
+            float3 a = ld3(acc, q);
+            float3 vc = ld3(vel_cot, q);
+            float3 v = axpy3(ld3(vel, q), a, K1);
+            float3 dc = axmy3(ld3(disp_cot, q), ld3(alpha, q), K1);
+            s0 += dot3d(vc, a);
+            d = axpy3(d, v, D);
+            vc = axmy3(vc, dc, D);
+            s1 += dot3d(dc, v);
+            st3(vel, q, v);
+            st3(disp, q, d);
+            st3(disp_cot, q, dc);
+            st3(vel_cot, q, vc);
+        }
+        Axis ax[3];
+        hot_enmesh(h, pmid, q, d, ax);
+        hot_deposit(h, ax, dens);
+    }
+    if (KD) {
+        double t0 = block_sum<PT>(s0, sh);
+        double t1 = block_sum<PT>(s1, sh);
+        if (threadIdx.x == 0) {
+            part[0 * PMAX + blockIdx.x] = t0;
+            part[1 * PMAX + blockIdx.x] = t1;
+        }
+    }
+}
+
+// Adjoint: gather the three acceleration meshes (new acc), the gather VJP
+// disp_cot term sum_j vc_j sum_k g_j[k] dfrac_k / cell (into alpha), and the
+// gather VJP mesh term mcot_j[k] += vc_j frac_k.  Partial dot slot 2 =
+// sum(vel_cot * acc_new).
+__global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__ pmid,
+                                              const float *__restrict__ disp,
+                                              const float *__restrict__ vel_cot, float *acc,
+                                              float *alpha, int64_t n, int64_t M,
+                                              const float *__restrict__ g, float *mcot,
+                                              double *part) {
+    __shared__ double sh[PT / 32];
+    double s2 = 0.0;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        Axis ax[3];
+        hot_enmesh(h, pmid, q, ld3(disp, q), ax);
+        float3 vc = ld3(vel_cot, q);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            int64_t c = hot_cell(h, ax, k);
+            float f = frac_of(ax, k);
+            float fg[3];
+            frac_grad_of(ax, k, fg);
+            float m0 = __ldg(g + c), m1 = __ldg(g + M + c), m2 = __ldg(g + 2 * M + c);
+            a0 = __fadd_rn(a0, __fmul_rn(m0, f));
+            a1 = __fadd_rn(a1, __fmul_rn(m1, f));
+            a2 = __fadd_rn(a2, __fmul_rn(m2, f));
+            float t = __fadd_rn(__fadd_rn(__fmul_rn(vc.x, m0), __fmul_rn(vc.y, m1)),
+                                __fmul_rn(vc.z, m2));
+            c0 = __fadd_rn(c0, __fmul_rn(t, fg[0]));
+            c1 = __fadd_rn(c1, __fmul_rn(t, fg[1]));
+            c2 = __fadd_rn(c2, __fmul_rn(t, fg[2]));
+            atomicAdd(mcot + c, __fmul_rn(vc.x, f));
+            atomicAdd(mcot + M + c, __fmul_rn(vc.y, f));
+            atomicAdd(mcot + 2 * M + c, __fmul_rn(vc.z, f));
+        }
+        float3 a = make_float3(a0, a1, a2);
+        st3(acc, q, a);
+        st3(alpha, q, make_float3(__fdiv_rn(c0, h.cell), __fdiv_rn(c1, h.cell),
+                                  __fdiv_rn(c2, h.cell)));
+        s2 += dot3d(vc, a);
+    }
+    double t2 = block_sum<PT>(s2, sh);
+    if (threadIdx.x == 0) part[2 * PMAX + blockIdx.x] = t2;
+}
+
+// Adjoint: scatter VJP disp_cot term sum_k (rho_cot[k] val) dfrac_k / cell
+// added into alpha, then optionally kick_adj(K2): vel += acc*K2,
+// disp_cot -= alpha*K2.
+template <bool KICK>
+__global__ void __launch_bounds__(PT) k_sadj(Hot h, const int16_t *__restrict__ pmid,
+                                             const float *__restrict__ disp, float *vel,
+                                             const float *__restrict__ acc, float *disp_cot,
+                                             float *alpha, int64_t n,
+                                             const float *__restrict__ rho_cot, float K2) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        Axis ax[3];
+        hot_enmesh(h, pmid, q, ld3(disp, q), ax);
+        float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            int64_t c = hot_cell(h, ax, k);
+            float fg[3];
+            frac_grad_of(ax, k, fg);
+            float t = __fmul_rn(__ldg(rho_cot + c), h.val);
+            c0 = __fadd_rn(c0, __fmul_rn(t, fg[0]));
+            c1 = __fadd_rn(c1, __fmul_rn(t, fg[1]));
+            c2 = __fadd_rn(c2, __fmul_rn(t, fg[2]));
+        }
+        float3 al = ld3(alpha, q);
+        al = make_float3(__fadd_rn(al.x, __fdiv_rn(c0, h.cell)),
+                         __fadd_rn(al.y, __fdiv_rn(c1, h.cell)),
+                         __fadd_rn(al.z, __fdiv_rn(c2, h.cell)));
+        st3(alpha, q, al);
+        if (KICK) {
+            st3(vel, q, axpy3(ld3(vel, q), ld3(acc, q), K2));
+            st3(disp_cot, q, axmy3(ld3(disp_cot, q), al, K2));
+        }
+    }
+}
+
+// Sums the per-block partials in a fixed order: dots[s] = sum of slot s for
+// s < nslots (dots may be NULL), and *om_out = om_scale * sum of slot 2
+// (om_out may be NULL).
+__global__ void k_finish(const double *part, int nblk, double *dots, int nslots, double *om_out,
+                         double om_scale) {
+    __shared__ double sh[32];
+    int last = nslots > 3 ? nslots : 3;
+    for (int s = 0; s < last; ++s) {
+        bool want = (dots && s < nslots) || (om_out && s == 2);
+        if (!want) continue;
+        double v = 0.0;
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += part[s * PMAX + b];
+        double t = block_sum<1024>(v, sh);
+        if (threadIdx.x == 0) {
+            if (dots && s < nslots) dots[s] = t;
+            if (om_out && s == 2) *om_out = om_scale * t;
+        }
+    }
+}
+
+// Elementwise leapfrog kernels of the generic API.
+__global__ void k_axpy(float *y, const float *__restrict__ x, int64_t n, float a) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = __fadd_rn(y[i], __fmul_rn(x[i], a));
+}
+
+// y += x*a; z -= w*a; partial sum(u * x) (u may equal the updated y/z: it
+// is read before any update of this element).  Covers kick_adj (y=vel,
+// x=acc, z=disp_cot, w=alpha, u=vel_cot) and drift_adj (y=disp, x=vel,
+// z=vel_cot, w=disp_cot, dot of the updated disp_cot... see callers).
+__global__ void k_kick_adj(float *vel, const float *__restrict__ acc, float *disp_cot,
+                           const float *__restrict__ alpha, const float *__restrict__ vel_cot,
+                           int64_t n, float K, double *part) {
+    __shared__ double sh[32];
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float a = acc[i];
+        vel[i] = __fadd_rn(vel[i], __fmul_rn(a, K));
+        disp_cot[i] = __fsub_rn(disp_cot[i], __fmul_rn(alpha[i], K));
+        s += (double)vel_cot[i] * (double)a;
+    }
+    double t = block_sum<PT>(s, sh);
+    if (part && threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void k_drift_adj(float *disp, const float *__restrict__ vel, float *vel_cot,
+                            const float *__restrict__ disp_cot, int64_t n, float D, double *part) {
+    __shared__ double sh[32];
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float v = vel[i];
+        float dc = disp_cot[i];
+        disp[i] = __fadd_rn(disp[i], __fmul_rn(v, D));
+        vel_cot[i] = __fsub_rn(vel_cot[i], __fmul_rn(dc, D));
+        s += (double)dc * (double)v;
+    }
+    double t = block_sum<PT>(s, sh);
+    if (part && threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void k_dot(const float *__restrict__ x, const float *__restrict__ y, int64_t n,
+                      double *part) {
+    __shared__ double sh[32];
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        s += (double)x[i] * (double)y[i];
+    double t = block_sum<PT>(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void k_reduce1(const double *part, int nblk, double *out) {
+    __shared__ double sh[32];
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += part[b];
+    double t = block_sum<1024>(v, sh);
+    if (threadIdx.x == 0) *out = t;
+}
+
+}  // namespace pmx
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+namespace {
+
+int grid_fill(int64_t n) { return stride_grid((n + 3) / 4, 256, 16); }
+
+// Per-device reduction scratch for the stand-alone dot entry points,
+// allocated once at their first use on a device.
+std::mutex g_scratch_mu;
+double *g_scratch[64] = {nullptr};
+
+int device_scratch(double **out) {
+    int dev = 0;
+    PMX_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(PMX_ERR_ARG, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch[dev]) {
+        if (cudaMalloc(&g_scratch[dev], PMAX * sizeof(double)) != cudaSuccess) {
+            g_scratch[dev] = nullptr;
+            cudaGetLastError();
+            return fail(PMX_ERR_NOMEM, "cannot allocate reduction scratch");
+        }
+    }
+    *out = g_scratch[dev];
+    return PMX_OK;
+}
+
+int check_hot(pmx_workspace *ws, const pmx_enmesh_spec *spec, const void *pmid, const void *disp,
+              int64_t n, int64_t ptcl_num, Hot *h) {
+    if (!ws) return fail(PMX_ERR_ARG, "null workspace");
+    if (!spec) return fail(PMX_ERR_ARG, "null spec");
+    if (spec->dim != 3) return fail(PMX_ERR_ARG, "the force path is 3-D");
+    if (spec->cell_size > 0 || spec->offset[0] != 0 || spec->offset[1] != 0 || spec->offset[2] != 0)
+        return fail(PMX_ERR_ARG, "the force path uses the default enmesh (offset 0, cell_size None)");
+    if (spec->mesh_shape[0] != ws->n0 || spec->mesh_shape[1] != ws->n1 || spec->mesh_shape[2] != ws->n2 ||
+        spec->wrap_shape[0] != ws->n0 || spec->wrap_shape[1] != ws->n1 || spec->wrap_shape[2] != ws->n2)
+        return fail(PMX_ERR_SHAPE, "mesh shape differs from the workspace's");
+    if (!(spec->conf_cell_size > 0)) return fail(PMX_ERR_ARG, "conf_cell_size must be > 0");
+    if (n < 0 || ptcl_num <= 0) return fail(PMX_ERR_ARG, "bad particle counts");
+    if (n > 0 && (!pmid || !disp)) return fail(PMX_ERR_ARG, "null pmid/disp");
+    int dev = 0;
+    PMX_CUDA(cudaGetDevice(&dev));
+    if (dev != ws->dev) return fail(PMX_ERR_ARG, "workspace belongs to another device");
+    for (int a = 0; a < 3; ++a) h->wrap[a] = spec->wrap_shape[a];
+    h->stride[2] = 1;
+    h->stride[1] = ws->n2;
+    h->stride[0] = ws->n1 * ws->n2;
+    h->cell = (float)spec->conf_cell_size;
+    h->val = (float)((double)ws->M / (double)ptcl_num);
+    return PMX_OK;
+}
+
+int ensure_ktab(pmx_workspace *ws, double cell, cudaStream_t st) {
+    if (ws->ktab_cell == cell) return PMX_OK;
+    double period = 2 * PI / cell;
+    float nyq = (float)(PI / cell);
+    float eps = nyq * 1.1920928955078125e-07f;
+    int tot = (int)(ws->n0 + ws->n1 + ws->n2h);
+    k_ktab<<<(tot + 255) / 256, 256, 0, st>>>(ws->ktab, (int)ws->n0, (int)ws->n1, (int)ws->n2,
+                                              period, nyq, eps);
+    PMX_LAUNCH_CHECK("k_ktab");
+    ws->ktab_cell = cell;
+    return PMX_OK;
+}
+
+int poisson_grid(pmx_workspace *ws) {
+    int64_t rows = ws->n0 * ws->n1;
+    int64_t blocks = (rows + 7) / 8;  // 8 warps per block
+    int64_t cap = (int64_t)device_sms() * 16;
+    return (int)(blocks < cap ? blocks : cap);
+}
+
+// Forward force up to the three acceleration meshes in ws->g.  With kd, the
+// kick/drift of the forward step (or kick_adj/drift_adj of the reverse step
+// when adj) precede the density deposit.
+int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t st) {
+    float s = (float)(1.5 * (double)(float)omega_m);
+    float c = (float)((double)s / (double)ws->M);
+    {
+        Stage sg(ws, 2, st, 0);
+        PMX_CUFFT(cufftSetStream(ws->r2c1, st));
+        PMX_CUFFT(cufftExecR2C(ws->r2c1, ws->dens, reinterpret_cast<cufftComplex *>(ws->ck)));
+    }
+    {
+        Stage sg(ws, 3, st, 1);
+        k_poisson_fwd<<<poisson_grid(ws), 256, 0, st>>>(ws->ck, ws->n0, ws->n1, ws->n2h, ws->Mc,
+                                                         ws->ktab, c);
+        PMX_LAUNCH_CHECK("k_poisson_fwd");
+    }
+    {
+        Stage sg(ws, 4, st, 0);
+        PMX_CUFFT(cufftSetStream(ws->c2r3, st));
+        PMX_CUFFT(cufftExecC2R(ws->c2r3, reinterpret_cast<cufftComplex *>(ws->ck), ws->g));
+    }
+    return PMX_OK;
+}
+
+// The force VJP tail after k_g3adj has filled ws->mcot: batched r2c, adjoint
+// Fourier kernel, c2r into ws->dens (now rho_cot, scale folded in).
+int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
+    float s = (float)(1.5 * (double)(float)omega_m);
+    float c = (float)((double)s / (double)ws->M);
+    {
+        Stage sg(ws, 8, st, 0);
+        PMX_CUFFT(cufftSetStream(ws->r2c3, st));
+        PMX_CUFFT(cufftExecR2C(ws->r2c3, ws->mcot, reinterpret_cast<cufftComplex *>(ws->ck)));
+    }
+    {
+        Stage sg(ws, 9, st, 1);
+        k_poisson_adj<<<poisson_grid(ws), 256, 0, st>>>(ws->ck, ws->n0, ws->n1, ws->n2h, ws->Mc,
+                                                         ws->ktab, c);
+        PMX_LAUNCH_CHECK("k_poisson_adj");
+    }
+    {
+        Stage sg(ws, 10, st, 0);
+        PMX_CUFFT(cufftSetStream(ws->c2r1, st));
+        PMX_CUFFT(cufftExecC2R(ws->c2r1, reinterpret_cast<cufftComplex *>(ws->ck), ws->dens));
+    }
+    return PMX_OK;
+}
+
+double om_scale(double omega_m) {
+    float s = (float)(1.5 * (double)(float)omega_m);
+    return 1.5 / (double)s;
+}
+
+int make_plan(cufftHandle *plan, const int64_t shape[3], cufftType type, int64_t batch,
+              size_t *work) {
+    PMX_CUFFT(cufftCreate(plan));
+    PMX_CUFFT(cufftSetAutoAllocation(*plan, 0));
+    long long n[3] = {shape[0], shape[1], shape[2]};
+    size_t w = 0;
+    PMX_CUFFT(cufftMakePlanMany64(*plan, 3, n, nullptr, 1, 0, nullptr, 1, 0, type, batch, &w));
+    *work = w;
+    return PMX_OK;
+}
+
+void ws_free(pmx_workspace *ws) {
+    if (!ws) return;
+    if (ws->have_r2c1) cufftDestroy(ws->r2c1);
+    if (ws->have_c2r3) cufftDestroy(ws->c2r3);
+    if (ws->have_r2c3) cufftDestroy(ws->r2c3);
+    if (ws->have_c2r1) cufftDestroy(ws->c2r1);
+    cudaFree(ws->dens);
+    cudaFree(ws->ck);
+    cudaFree(ws->g);
+    cudaFree(ws->mcot);
+    cudaFree(ws->ktab);
+    cudaFree(ws->part);
+    cudaFree(ws->fft_work);
+    for (auto &r : ws->recs) {
+        cudaEventDestroy(r.b);
+        cudaEventDestroy(r.e);
+    }
+    for (auto e : ws->pool) cudaEventDestroy(e);
+    delete ws;
+}
+
+size_t buffers_bytes(const int64_t s[3], int32_t flags) {
+    int64_t M = s[0] * s[1] * s[2], Mc = s[0] * s[1] * (s[2] / 2 + 1);
+    size_t b = (size_t)M * 4 + (size_t)Mc * 8 * 3 + (size_t)M * 4 * 3;
+    if (flags & PMX_WS_ADJOINT) b += (size_t)M * 4 * 3;
+    b += (size_t)2 * (s[0] + s[1] + s[2] / 2 + 1) * 4 + (size_t)NSLOT * PMAX * 8;
+    return b;
+}
+
+int check_shape(const int64_t s[3]) {
+    for (int a = 0; a < 3; ++a)
+        if (s[a] < 1 || s[a] > (1 << 20)) return fail(PMX_ERR_SHAPE, "bad mesh shape");
+    return PMX_OK;
+}
+
+}  // namespace
+
+extern "C" int pmx_workspace_bytes(const int64_t mesh_shape[3], int32_t flags, size_t *bytes) {
+    if (!mesh_shape || !bytes) return fail(PMX_ERR_ARG, "null argument");
+    int st = check_shape(mesh_shape);
+    if (st) return st;
+    size_t total = buffers_bytes(mesh_shape, flags), wmax = 0;
+    cufftType types[4] = {CUFFT_R2C, CUFFT_C2R, CUFFT_R2C, CUFFT_C2R};
+    int64_t batches[4] = {1, 3, 3, 1};
+    int nplans = (flags & PMX_WS_ADJOINT) ? 4 : 2;
+    for (int i = 0; i < nplans; ++i) {
+        int n[3] = {(int)mesh_shape[0], (int)mesh_shape[1], (int)mesh_shape[2]};
+        size_t w = 0;
+        PMX_CUFFT(cufftEstimateMany(3, n, nullptr, 1, 0, nullptr, 1, 0, types[i],
+                                    (int)batches[i], &w));
+        if (w > wmax) wmax = w;
+    }
+    *bytes = total + wmax;
+    return PMX_OK;
+}
+
+extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
+                                    pmx_workspace **out) {
+    if (!mesh_shape || !out) return fail(PMX_ERR_ARG, "null argument");
+    int st = check_shape(mesh_shape);
+    if (st) return st;
+    pmx_workspace *ws = new pmx_workspace();
+    ws->flags = flags;
+    ws->n0 = mesh_shape[0];
+    ws->n1 = mesh_shape[1];
+    ws->n2 = mesh_shape[2];
+    ws->n2h = ws->n2 / 2 + 1;
+    ws->M = ws->n0 * ws->n1 * ws->n2;
+    ws->Mc = ws->n0 * ws->n1 * ws->n2h;
+    if (cudaGetDevice(&ws->dev) != cudaSuccess) {
+        delete ws;
+        return fail(PMX_ERR_CUDA, "cudaGetDevice failed");
+    }
+    auto alloc = [&](void **p, size_t b) -> int {
+        if (cudaMalloc(p, b) != cudaSuccess) {
+            cudaGetLastError();
+            *p = nullptr;
+            return fail(PMX_ERR_NOMEM, "workspace allocation of " + std::to_string(b) + " bytes failed");
+        }
+        return PMX_OK;
+    };
+    int64_t ktn = 2 * (ws->n0 + ws->n1 + ws->n2h);
+    if ((st = alloc((void **)&ws->dens, ws->M * 4)) || (st = alloc((void **)&ws->ck, ws->Mc * 8 * 3)) ||
+        (st = alloc((void **)&ws->g, ws->M * 4 * 3)) || (st = alloc((void **)&ws->ktab, ktn * 4)) ||
+        (st = alloc((void **)&ws->part, NSLOT * PMAX * 8)) ||
+        ((flags & PMX_WS_ADJOINT) && (st = alloc((void **)&ws->mcot, ws->M * 4 * 3)))) {
+        ws_free(ws);
+        return st;
+    }
+    size_t w1 = 0, w2 = 0, w3 = 0, w4 = 0;
+    int64_t shp[3] = {ws->n0, ws->n1, ws->n2};
+    if ((st = make_plan(&ws->r2c1, shp, CUFFT_R2C, 1, &w1))) { ws_free(ws); return st; }
+    ws->have_r2c1 = true;
+    if ((st = make_plan(&ws->c2r3, shp, CUFFT_C2R, 3, &w2))) { ws_free(ws); return st; }
+    ws->have_c2r3 = true;
+    if (flags & PMX_WS_ADJOINT) {
+        if ((st = make_plan(&ws->r2c3, shp, CUFFT_R2C, 3, &w3))) { ws_free(ws); return st; }
+        ws->have_r2c3 = true;
+        if ((st = make_plan(&ws->c2r1, shp, CUFFT_C2R, 1, &w4))) { ws_free(ws); return st; }
+        ws->have_c2r1 = true;
+    }
+    size_t wmax = w1;
+    if (w2 > wmax) wmax = w2;
+    if (w3 > wmax) wmax = w3;
+    if (w4 > wmax) wmax = w4;
+    if (wmax > 0 && (st = alloc(&ws->fft_work, wmax))) { ws_free(ws); return st; }
+    ws->fft_work_bytes = wmax;
+    cufftHandle plans[4] = {ws->r2c1, ws->c2r3, ws->r2c3, ws->c2r1};
+    bool have[4] = {ws->have_r2c1, ws->have_c2r3, ws->have_r2c3, ws->have_c2r1};
+    for (int i = 0; i < 4; ++i) {
+        if (!have[i]) continue;
+        cufftResult r = cufftSetWorkArea(plans[i], ws->fft_work);
+        if (r != CUFFT_SUCCESS) {
+            ws_free(ws);
+            return fail(PMX_ERR_CUFFT, std::string("cufftSetWorkArea: ") + cufft_name(r));
+        }
+    }
+    *out = ws;
+    return PMX_OK;
+}
+
+extern "C" int pmx_workspace_destroy(pmx_workspace *ws) {
+    if (!ws) return PMX_OK;
+    cudaDeviceSynchronize();
+    ws_free(ws);
+    return PMX_OK;
+}
+
+extern "C" int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int16_t *pmid,
+                         const float *disp, int64_t n, int64_t ptcl_num, double omega_m,
+                         float *acc, void *stream) {
+    Hot h;
+    int st = check_hot(ws, spec, pmid, disp, n, ptcl_num, &h);
+    if (st) return st;
+    if (n > 0 && !acc) return fail(PMX_ERR_ARG, "null acc");
+    cudaStream_t s = as_stream(stream);
+    if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
+    {
+        Stage sg(ws, 0, s, 1);
+        k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
+        PMX_LAUNCH_CHECK("k_fill");
+    }
+    if (n > 0) {
+        {
+            Stage sg(ws, 1, s, 1);
+            k_kds<false><<<stride_grid(n, PT), PT, 0, s>>>(h, pmid, const_cast<float *>(disp), nullptr,
+                                                          nullptr, n, 0.f, 0.f, ws->dens);
+            PMX_LAUNCH_CHECK("k_kds");
+        }
+    }
+    if ((st = force_meshes(ws, h, omega_m, s))) return st;
+    if (n > 0) {
+        {
+            Stage sg(ws, 5, s, 1);
+            k_gather3<false><<<stride_grid(n, PT), PT, 0, s>>>(h, pmid, disp, nullptr, acc, n, ws->M,
+                                                              ws->g, 0.f);
+            PMX_LAUNCH_CHECK("k_gather3");
+        }
+    }
+    return PMX_OK;
+}
+
+extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int16_t *pmid,
+                             const float *disp, int64_t n, int64_t ptcl_num, double omega_m,
+                             const float *acc_cot, float *acc, float *disp_cot,
+                             double *omega_m_cot, void *stream) {
+    Hot h;
+    int st = check_hot(ws, spec, pmid, disp, n, ptcl_num, &h);
+    if (st) return st;
+    if (!(ws->flags & PMX_WS_ADJOINT)) return fail(PMX_ERR_ARG, "workspace lacks PMX_WS_ADJOINT");
+    if (n > 0 && (!acc_cot || !acc || !disp_cot)) return fail(PMX_ERR_ARG, "null acc_cot/acc/disp_cot");
+    cudaStream_t s = as_stream(stream);
+    if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
+    {
+        Stage sg(ws, 0, s, 2);
+        k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
+        k_fill<<<grid_fill(3 * ws->M), 256, 0, s>>>(ws->mcot, 0.f, 3 * ws->M);
+        PMX_LAUNCH_CHECK("k_fill");
+    }
+    int G = stride_grid(n, PT);
+    if (G > PMAX) G = PMAX;
+    if (n > 0) {
+        {
+            Stage sg(ws, 1, s, 1);
+            k_kds<false><<<G, PT, 0, s>>>(h, pmid, const_cast<float *>(disp), nullptr, nullptr, n, 0.f,
+                                          0.f, ws->dens);
+            PMX_LAUNCH_CHECK("k_kds");
+        }
+    }
+    if ((st = force_meshes(ws, h, omega_m, s))) return st;
+    if (n > 0) {
+        {
+            Stage sg(ws, 7, s, 1);
+            k_g3adj<<<G, PT, 0, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M, ws->g, ws->mcot,
+                                     ws->part);
+            PMX_LAUNCH_CHECK("k_g3adj");
+        }
+    }
+    if ((st = force_adj_meshes(ws, omega_m, s))) return st;
+    if (n > 0) {
+        {
+            Stage sg(ws, 11, s, 1);
+            k_sadj<false><<<G, PT, 0, s>>>(h, pmid, disp, nullptr, nullptr, nullptr, disp_cot, n,
+                                           ws->dens, 0.f);
+            PMX_LAUNCH_CHECK("k_sadj");
+        }
+    }
+    if (omega_m_cot) {
+        if (n == 0) {
+            PMX_CUDA(cudaMemsetAsync(omega_m_cot, 0, sizeof(double), s));
+        } else {
+            {
+                Stage sg(ws, 12, s, 1);
+                k_finish<<<1, 1024, 0, s>>>(ws->part, G, nullptr, 0, omega_m_cot, om_scale(omega_m));
+                PMX_LAUNCH_CHECK("k_finish");
+            }
+        }
+    }
+    return PMX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// leapfrog entry points
+// ---------------------------------------------------------------------------
+
+extern "C" int pmx_kick(float *vel, const float *acc, int64_t n3, float factor, void *stream) {
+    if (n3 < 0) return fail(PMX_ERR_ARG, "negative size");
+    if (n3 == 0) return PMX_OK;
+    if (!vel || !acc) return fail(PMX_ERR_ARG, "null vel/acc");
+    k_axpy<<<stride_grid(n3, PT), PT, 0, as_stream(stream)>>>(vel, acc, n3, factor);
+    PMX_LAUNCH_CHECK("k_axpy");
+    return PMX_OK;
+}
+
+extern "C" int pmx_drift(float *disp, const float *vel, int64_t n3, float factor, void *stream) {
+    if (n3 < 0) return fail(PMX_ERR_ARG, "negative size");
+    if (n3 == 0) return PMX_OK;
+    if (!disp || !vel) return fail(PMX_ERR_ARG, "null disp/vel");
+    k_axpy<<<stride_grid(n3, PT), PT, 0, as_stream(stream)>>>(disp, vel, n3, factor);
+    PMX_LAUNCH_CHECK("k_axpy");
+    return PMX_OK;
+}
+
+extern "C" int pmx_kick_adj(float *vel, const float *acc, float *disp_cot, const float *acc_cot,
+                            const float *vel_cot, int64_t n3, float factor, double *dot,
+                            void *stream) {
+    if (n3 < 0) return fail(PMX_ERR_ARG, "negative size");
+    cudaStream_t s = as_stream(stream);
+    if (n3 == 0) {
+        if (dot) PMX_CUDA(cudaMemsetAsync(dot, 0, sizeof(double), s));
+        return PMX_OK;
+    }
+    if (!vel || !acc || !disp_cot || !acc_cot || !vel_cot) return fail(PMX_ERR_ARG, "null array");
+    double *scr = nullptr;
+    int st;
+    if (dot && (st = device_scratch(&scr))) return st;
+    int G = stride_grid(n3, PT);
+    if (G > PMAX) G = PMAX;
+    k_kick_adj<<<G, PT, 0, s>>>(vel, acc, disp_cot, acc_cot, vel_cot, n3, factor, scr);
+    PMX_LAUNCH_CHECK("k_kick_adj");
+    if (dot) {
+        k_reduce1<<<1, 1024, 0, s>>>(scr, G, dot);
+        PMX_LAUNCH_CHECK("k_reduce1");
+    }
+    return PMX_OK;
+}
+
+extern "C" int pmx_drift_adj(float *disp, const float *vel, float *vel_cot, const float *disp_cot,
+                             int64_t n3, float factor, double *dot, void *stream) {
+    if (n3 < 0) return fail(PMX_ERR_ARG, "negative size");
+    cudaStream_t s = as_stream(stream);
+    if (n3 == 0) {
+        if (dot) PMX_CUDA(cudaMemsetAsync(dot, 0, sizeof(double), s));
+        return PMX_OK;
+    }
+    if (!disp || !vel || !vel_cot || !disp_cot) return fail(PMX_ERR_ARG, "null array");
+    double *scr = nullptr;
+    int st;
+    if (dot && (st = device_scratch(&scr))) return st;
+    int G = stride_grid(n3, PT);
+    if (G > PMAX) G = PMAX;
+    k_drift_adj<<<G, PT, 0, s>>>(disp, vel, vel_cot, disp_cot, n3, factor, scr);
+    PMX_LAUNCH_CHECK("k_drift_adj");
+    if (dot) {
+        k_reduce1<<<1, 1024, 0, s>>>(scr, G, dot);
+        PMX_LAUNCH_CHECK("k_reduce1");
+    }
+    return PMX_OK;
+}
+
+extern "C" int pmx_dot(const float *x, const float *y, int64_t n, double *out, void *stream) {
+    if (n < 0 || !out) return fail(PMX_ERR_ARG, "bad dot arguments");
+    cudaStream_t s = as_stream(stream);
+    if (n == 0) {
+        PMX_CUDA(cudaMemsetAsync(out, 0, sizeof(double), s));
+        return PMX_OK;
+    }
+    if (!x || !y) return fail(PMX_ERR_ARG, "null x/y");
+    double *scr = nullptr;
+    int st;
+    if ((st = device_scratch(&scr))) return st;
+    int G = stride_grid(n, PT);
+    if (G > PMAX) G = PMAX;
+    k_dot<<<G, PT, 0, s>>>(x, y, n, scr);
+    PMX_LAUNCH_CHECK("k_dot");
+    k_reduce1<<<1, 1024, 0, s>>>(scr, G, out);
+    PMX_LAUNCH_CHECK("k_reduce1");
+    return PMX_OK;
+}
+
+extern "C" int pmx_nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int16_t *pmid,
+                              float *disp, float *vel, float *acc, int64_t n, int64_t ptcl_num,
+                              const float factors[3], double omega_m, void *stream) {
+    Hot h;
+    int st = check_hot(ws, spec, pmid, disp, n, ptcl_num, &h);
+    if (st) return st;
+    if (!factors) return fail(PMX_ERR_ARG, "null factors");
+    if (n > 0 && (!vel || !acc)) return fail(PMX_ERR_ARG, "null vel/acc");
+    cudaStream_t s = as_stream(stream);
+    if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
+    {
+        Stage sg(ws, 0, s, 1);
+        k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
+        PMX_LAUNCH_CHECK("k_fill");
+    }
+    int G = stride_grid(n, PT);
+    if (n > 0) {
+        {
+            Stage sg(ws, 1, s, 1);
+            k_kds<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, factors[0], factors[1], ws->dens);
+            PMX_LAUNCH_CHECK("k_kds");
+        }
+    }
+    if ((st = force_meshes(ws, h, omega_m, s))) return st;
+    if (n > 0) {
+        {
+            Stage sg(ws, 5, s, 1);
+            k_gather3<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, ws->M, ws->g, factors[2]);
+            PMX_LAUNCH_CHECK("k_gather3");
+        }
+    }
+    return PMX_OK;
+}
+
+extern "C" int pmx_nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                                  const int16_t *pmid, float *disp, float *vel, float *acc,
+                                  float *disp_cot, float *vel_cot, float *acc_cot, int64_t n,
+                                  int64_t ptcl_num, const float factors[3], double omega_m,
+                                  double *dots, void *stream) {
+    Hot h;
+    int st = check_hot(ws, spec, pmid, disp, n, ptcl_num, &h);
+    if (st) return st;
+    if (!(ws->flags & PMX_WS_ADJOINT)) return fail(PMX_ERR_ARG, "workspace lacks PMX_WS_ADJOINT");
+    if (!factors || !dots) return fail(PMX_ERR_ARG, "null factors/dots");
+    if (n > 0 && (!vel || !acc || !disp_cot || !vel_cot || !acc_cot))
+        return fail(PMX_ERR_ARG, "null particle array");
+    cudaStream_t s = as_stream(stream);
+    if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
+    {
+        Stage sg(ws, 0, s, 2);
+        k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
+        k_fill<<<grid_fill(3 * ws->M), 256, 0, s>>>(ws->mcot, 0.f, 3 * ws->M);
+        PMX_LAUNCH_CHECK("k_fill");
+    }
+    if (n == 0) {
+        PMX_CUDA(cudaMemsetAsync(dots, 0, 4 * sizeof(double), s));
+        return PMX_OK;
+    }
+    int G = stride_grid(n, PT);
+    if (G > PMAX) G = PMAX;
+    {
+        Stage sg(ws, 6, s, 1);
+        k_ka<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n, factors[0],
+                                    factors[1], ws->dens, ws->part);
+        PMX_LAUNCH_CHECK("k_ka");
+    }
+    if ((st = force_meshes(ws, h, omega_m, s))) return st;
+    {
+        Stage sg(ws, 7, s, 1);
+        k_g3adj<<<G, PT, 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M, ws->g, ws->mcot,
+                                 ws->part);
+        PMX_LAUNCH_CHECK("k_g3adj");
+    }
+    if ((st = force_adj_meshes(ws, omega_m, s))) return st;
+    {
+        Stage sg(ws, 11, s, 1);
+        k_sadj<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n, ws->dens,
+                                      factors[2]);
+        PMX_LAUNCH_CHECK("k_sadj");
+    }
+    {
+        Stage sg(ws, 12, s, 1);
+        k_finish<<<1, 1024, 0, s>>>(ws->part, G, dots, 3, dots + 3, om_scale(omega_m));
+        PMX_LAUNCH_CHECK("k_finish");
+    }
+    return PMX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// stage profiler
+// ---------------------------------------------------------------------------
+
+extern "C" int pmx_profile_enable(pmx_workspace *ws, int on) {
+    if (!ws) return fail(PMX_ERR_ARG, "null workspace");
+    ws->prof_on = on != 0;
+    return PMX_OK;
+}
+
+extern "C" int pmx_profile_read(pmx_workspace *ws, double *ms, int64_t *calls, int64_t *launches) {
+    if (!ws) return fail(PMX_ERR_ARG, "null workspace");
+    double acc[PMX_PROF_STAGES] = {0};
+    int64_t cnt[PMX_PROF_STAGES] = {0};
+    int st = PMX_OK;
+    for (auto &r : ws->recs) {
+        float t = 0.f;
+        cudaError_t e = cudaEventSynchronize(r.e);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, r.b, r.e);
+        if (e != cudaSuccess && st == PMX_OK) st = cuda_status(e, "pmx_profile_read");
+        acc[r.stage] += t;
+        cnt[r.stage] += 1;
+        ws->pool.push_back(r.b);
+        ws->pool.push_back(r.e);
+    }
+    ws->recs.clear();
+    for (int i = 0; i < PMX_PROF_STAGES; ++i) {
+        if (ms) ms[i] = acc[i];
+        if (calls) calls[i] = cnt[i];
+    }
+    if (launches) *launches = ws->launches;
+    ws->launches = 0;
+    return st;
+}
+
+extern "C" const char *pmx_profile_stage_name(int i) {
+    if (i < 0 || i >= PMX_PROF_STAGES) return nullptr;
+    return kStageNames[i];
+}

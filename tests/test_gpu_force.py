@@ -1,0 +1,182 @@
+"""GPU parity of the Poisson force, the leapfrog and the reversible adjoint
+against the CPU oracle, through the C ABI and the pmwd-style API."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cosmo as oc, ics, nbody as onb, pm
+import pmwd_gb300 as pg
+from pmwd_gb300 import _lib
+import importlib
+gnb = importlib.import_module("pmwd_gb300.nbody")
+
+pytestmark = pytest.mark.gpu
+
+RTOL_ACC = 1e-5       # single force step, relative L2 (float32 FFT rounding)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def T(x, dev):
+    return torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+
+
+def make(ptcl, mesh, spacing, std, seed=0, a_step=1 / 8):
+    oconf = oc.OConf(spacing, ptcl, mesh, float_dtype=np.float32, a_nbody_maxstep=a_step)
+    gconf = pg.Configuration(spacing, ptcl, mesh, a_nbody_maxstep=a_step)
+    pmid, disp = ics.gen_grid(oconf)
+    rng = np.random.default_rng(seed)
+    disp = (disp + rng.normal(0, std, disp.shape)).astype(np.float32)
+    vel = rng.normal(0, 0.1, disp.shape).astype(np.float32)
+    return oconf, gconf, pmid, disp, vel
+
+
+@pytest.mark.parametrize('ptcl, mesh, spacing', [((16, 16, 16), 2, 1.0), ((12, 20, 8), 1, 2.0),
+                                                  ((32, 32, 32), 1, 4.0)])
+def test_force_matches_oracle(cuda, ptcl, mesh, spacing):
+    oconf, gconf, pmid, disp, vel = make(ptcl, mesh, spacing, 1.5 * spacing)
+    acc_o = pm.gravity(pmid, disp, 0.3, oconf)
+    ws = _lib.workspace(gconf.mesh_shape)
+    spec = _lib.make_spec(3, gconf.mesh_shape, gconf.mesh_shape, gconf.cell_size)
+    acc = torch.empty((len(pmid), 3), dtype=torch.float32, device=cuda)
+    _lib.call('pmx_force', ws.handle, spec, _lib.ptr(T(pmid, cuda)), _lib.ptr(T(disp, cuda)),
+              len(pmid), gconf.ptcl_num, 0.3, _lib.ptr(acc), _lib.stream_ptr(cuda))
+    assert rel_l2(acc.cpu().numpy(), acc_o) < RTOL_ACC
+
+
+@pytest.mark.parametrize('ptcl, mesh', [((16, 16, 16), 2), ((10, 12, 14), 1)])
+def test_force_vjp_matches_oracle(cuda, ptcl, mesh):
+    oconf, gconf, pmid, disp, vel = make(ptcl, mesh, 2.0, 2.0)
+    cot = np.random.default_rng(9).normal(size=disp.shape).astype(np.float32)
+    oconf64 = oc.OConf(2.0, ptcl, mesh, float_dtype=np.float64)
+    acc_o, dc_o, om_o = pm.gravity_vjp(pmid, disp.astype(np.float64), 0.3, oconf64,
+                                       cot.astype(np.float64))
+    ws = _lib.workspace(gconf.mesh_shape)
+    spec = _lib.make_spec(3, gconf.mesh_shape, gconf.mesh_shape, gconf.cell_size)
+    n = len(pmid)
+    acc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+    dc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+    om = torch.zeros((), dtype=torch.float64, device=cuda)
+    _lib.call('pmx_force_vjp', ws.handle, spec, _lib.ptr(T(pmid, cuda)), _lib.ptr(T(disp, cuda)),
+              n, gconf.ptcl_num, 0.3, _lib.ptr(T(cot, cuda)), _lib.ptr(acc), _lib.ptr(dc),
+              _lib.ptr(om), _lib.stream_ptr(cuda))
+    assert rel_l2(acc.cpu().numpy(), acc_o) < RTOL_ACC
+    assert rel_l2(dc.cpu().numpy(), dc_o) < 1e-4
+    assert abs(float(om) / om_o - 1) < 1e-4
+
+
+def test_gravity_autograd_api(cuda):
+    """gravity() through torch autograd equals the explicit VJP."""
+    oconf, gconf, pmid, disp, vel = make((16, 16, 16), 2, 1.0, 1.0)
+    cosmo = pg.SimpleLCDM(gconf)
+    Om = cosmo.Omega_m.clone().requires_grad_(True)
+    cosmo = cosmo.replace(Omega_m=Om)
+    D = T(disp, cuda).requires_grad_(True)
+    ptcl = pg.Particles(gconf, T(pmid, cuda), D)
+    acc = pg.gravity(0.5, ptcl, cosmo, gconf)
+    cot = torch.randn_like(acc)
+    (acc * cot).sum().backward()
+    oconf64 = oc.OConf(1.0, (16, 16, 16), 2, float_dtype=np.float64)
+    _, dc_o, om_o = pm.gravity_vjp(pmid, disp.astype(np.float64), 0.3, oconf64,
+                                   cot.cpu().numpy().astype(np.float64))
+    assert rel_l2(D.grad.cpu().numpy(), dc_o) < 1e-4
+    assert abs(float(Om.grad) / om_o - 1) < 1e-4
+
+
+def _run_gpu_nbody(gconf, pmid, disp, vel, cosmo, dev):
+    ptcl = pg.Particles(gconf, T(pmid, dev), T(disp, dev), vel=T(vel, dev))
+    out, _ = pg.nbody(ptcl, None, cosmo, gconf)
+    return out
+
+
+@pytest.fixture(scope='module')
+def nb_case():
+    oconf, gconf, pmid, disp, vel = make((16, 16, 16), 2, 4.0, 0.5, a_step=1 / 8)
+    ocos = oc.with_tables(oc.simple_lcdm(), oconf)
+    gcos = pg.boltzmann(pg.SimpleLCDM(gconf), gconf)
+    return oconf, gconf, pmid, disp, vel, ocos, gcos
+
+
+def test_nbody_forward_matches_oracle(cuda, nb_case):
+    oconf, gconf, pmid, disp, vel, ocos, gcos = nb_case
+    st = onb.nbody(onb.State(pmid, disp, vel), ocos, oconf)
+    out = _run_gpu_nbody(gconf, pmid, disp, vel, gcos, cuda)
+    # position RMS within 1e-3 of the particle spacing (spec tier 3)
+    rms = np.sqrt(np.mean((out.disp.cpu().numpy().astype(np.float64) - st.disp) ** 2))
+    assert rms < 1e-3 * oconf.ptcl_spacing
+    assert rel_l2(out.disp.cpu().numpy(), st.disp) < 1e-4
+    assert rel_l2(out.vel.cpu().numpy(), st.vel) < 1e-4
+    assert rel_l2(out.acc.cpu().numpy(), st.acc) < 1e-4
+
+
+def test_fused_step_equals_generic_ops(cuda, nb_case):
+    """The fused step kernels reproduce the reference op sequence run op by
+    op (bit-identical float32 arithmetic except for atomic order)."""
+    oconf, gconf, pmid, disp, vel, ocos, gcos = nb_case
+    fused = _run_gpu_nbody(gconf, pmid, disp, vel, gcos, cuda)
+    gconf2 = gconf.replace(symp_splits=((0.0, 0.5), (1.0, 0.5), (0.0, 0.0)))
+    assert not gnb._is_fused(gconf2)
+    generic = _run_gpu_nbody(gconf2, pmid, disp, vel, pg.boltzmann(pg.SimpleLCDM(gconf2), gconf2),
+                             cuda)
+    assert rel_l2(generic.disp.cpu().numpy(), fused.disp.cpu().numpy()) < 1e-6
+    assert rel_l2(generic.vel.cpu().numpy(), fused.vel.cpu().numpy()) < 1e-6
+
+
+def test_factors_match_oracle(nb_case):
+    oconf, gconf, pmid, disp, vel, ocos, gcos = nb_case
+    ops = gnb.forward_ops(gconf)
+    f = gnb.op_factors(ops, gcos, gconf).detach().numpy()
+    ref = []
+    for o in ops:
+        if o[0] == 'kick':
+            ref.append(oc.kick_factor(*o[1:], ocos, oconf))
+        elif o[0] == 'drift':
+            ref.append(oc.drift_factor(*o[1:], ocos, oconf))
+    np.testing.assert_allclose(f, ref, rtol=1e-8)
+    adj = gnb.op_factors(gnb.adjoint_ops(gconf), gcos, gconf).detach().numpy().reshape(-1, 3)
+    fwd = f.reshape(-1, 3)[::-1]
+    np.testing.assert_array_equal(adj[:, 0], -fwd[:, 2])
+    np.testing.assert_array_equal(adj[:, 1], -fwd[:, 1])
+    np.testing.assert_array_equal(adj[:, 2], -fwd[:, 0])
+
+
+def test_nbody_adjoint_matches_oracle(cuda, nb_case):
+    """Reversible adjoint: cotangents at the start, per-factor
+    sensitivities and the Omega_m force term against the oracle's
+    nbody_adj (which itself matches float64 autograd)."""
+    oconf, gconf, pmid, disp, vel, ocos, gcos = nb_case
+    rng = np.random.default_rng(11)
+    dcot = rng.normal(size=disp.shape).astype(np.float32)
+    vcot = rng.normal(size=disp.shape).astype(np.float32)
+    oconf64 = oc.OConf(oconf.ptcl_spacing, oconf.ptcl_grid_shape, oconf.mesh_shape,
+                       float_dtype=np.float64, a_nbody_maxstep=oconf.a_nbody_maxstep)
+    ocos64 = oc.with_tables(oc.simple_lcdm(), oconf64)
+    st1 = onb.nbody(onb.State(pmid, disp.astype(np.float64), vel.astype(np.float64)), ocos64,
+                    oconf64)
+    st0, cot0, sens = onb.nbody_adj(st1, onb.Cot(dcot.astype(np.float64), vcot.astype(np.float64)),
+                                    ocos64, oconf64)
+
+    D = T(disp, cuda).requires_grad_(True)
+    V = T(vel, cuda).requires_grad_(True)
+    Om = gcos.Omega_m.clone().requires_grad_(True)
+    cos = gcos.replace(Omega_m=Om)
+    ptcl = pg.Particles(gconf, T(pmid, cuda), D, vel=V)
+    out, _ = pg.nbody(ptcl, None, cos, gconf)
+    ((out.disp * T(dcot, cuda)).sum() + (out.vel * T(vcot, cuda)).sum()).backward()
+    assert rel_l2(D.grad.cpu().numpy(), cot0.disp) < 1e-3
+    assert rel_l2(V.grad.cpu().numpy(), cot0.vel) < 1e-3
+
+    # explicit adjoint API: per-factor sensitivities and the Omega_m term
+    ptcl1 = out.replace(disp=out.disp.detach(), vel=out.vel.detach(), acc=out.acc.detach())
+    cot = pg.Particles(gconf, ptcl1.pmid, T(dcot, cuda), vel=T(vcot, cuda))
+    p0, c0, fgrad, omg = gnb.nbody_adj(ptcl1, cot, None, gcos, gconf)
+    ref = np.array([s for *_, s in sens['factors']])
+    assert rel_l2(fgrad.numpy(), ref) < 1e-3
+    assert abs(float(omg) / sens['Omega_m'] - 1) < 1e-3
+    # the reconstructed initial state returns to the start
+    assert rel_l2(p0.disp.cpu().numpy(), disp) < 1e-4
