@@ -112,7 +112,14 @@ def check(status, what=''):
 
 
 def call(name, *args):
-    check(getattr(load(), name)(*args), name)
+    """Call an entry point.  Tensor arguments are passed as device pointers
+    and stay referenced until the call has enqueued its work, so a temporary
+    cannot be freed (and its memory reused by the caching allocator) before
+    the kernels that read it are on the stream."""
+    keep = [a for a in args if torch.is_tensor(a)]
+    conv = [c_p(a.data_ptr()) if torch.is_tensor(a) else a for a in args]
+    check(getattr(load(), name)(*conv), name)
+    del keep
 
 
 def ptr(t):

@@ -30,7 +30,8 @@ def interp(x, xp, fp):
     x = torch.as_tensor(x, dtype=DT, device=fp.device)
     xp = xp.to(device=fp.device, dtype=DT)
     n = xp.shape[0]
-    i = torch.clamp(torch.searchsorted(xp, x.detach().reshape(-1), right=True), 1, n - 1)
+    i = torch.clamp(torch.searchsorted(xp, x.detach().reshape(-1).contiguous(), right=True),
+                    1, n - 1)
     i = i.reshape(x.shape)
     df = fp[i] - fp[i - 1]
     dx = xp[i] - xp[i - 1]

@@ -78,7 +78,7 @@ class _GravityFn(torch.autograd.Function):
         disp_cot = torch.empty_like(disp)
         om = torch.empty((), dtype=torch.float64, device=disp.device)
         _lib.call('pmx_force_vjp', ws.handle, spec, _lib.ptr(pmid), _lib.ptr(disp), n,
-                  conf.ptcl_num, ctx.Om, _lib.ptr(acc_cot.contiguous()), _lib.ptr(acc),
+                  conf.ptcl_num, ctx.Om, acc_cot.contiguous(), _lib.ptr(acc),
                   _lib.ptr(disp_cot), _lib.ptr(om), _lib.stream_ptr(disp.device))
         om_cot = om.cpu() if ctx.needs_input_grad[1] else None
         return disp_cot, om_cot, None, None

@@ -129,8 +129,8 @@ def ptcl_enmesh(ptcl, conf, offset=0, cell_size=None, mesh_shape=None, wrap=True
     ind = torch.empty((n, nk, dim), dtype=torch.int32, device=dev)
     frac = torch.empty((n, nk), dtype=torch.float32, device=dev)
     fg = torch.empty((n, nk, dim), dtype=torch.float32, device=dev) if grad else None
-    _lib.call('pmx_enmesh', spec, _lib.ptr(ptcl.pmid.contiguous()),
-              _lib.ptr(ptcl.disp.contiguous()), n, _lib.ptr(ind), _lib.ptr(frac), _lib.ptr(fg),
+    _lib.call('pmx_enmesh', spec, ptcl.pmid.contiguous(),
+              ptcl.disp.contiguous(), n, _lib.ptr(ind), _lib.ptr(frac), _lib.ptr(fg),
               _lib.stream_ptr(dev))
     ind = ind.to(conf.pmid_dtype)
     return (ind, frac, fg) if grad else (ind, frac)

@@ -44,7 +44,7 @@ def test_force_matches_oracle(cuda, ptcl, mesh, spacing):
     ws = _lib.workspace(gconf.mesh_shape)
     spec = _lib.make_spec(3, gconf.mesh_shape, gconf.mesh_shape, gconf.cell_size)
     acc = torch.empty((len(pmid), 3), dtype=torch.float32, device=cuda)
-    _lib.call('pmx_force', ws.handle, spec, _lib.ptr(T(pmid, cuda)), _lib.ptr(T(disp, cuda)),
+    _lib.call('pmx_force', ws.handle, spec, T(pmid, cuda), T(disp, cuda),
               len(pmid), gconf.ptcl_num, 0.3, _lib.ptr(acc), _lib.stream_ptr(cuda))
     assert rel_l2(acc.cpu().numpy(), acc_o) < RTOL_ACC
 
@@ -62,8 +62,8 @@ def test_force_vjp_matches_oracle(cuda, ptcl, mesh):
     acc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
     dc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
     om = torch.zeros((), dtype=torch.float64, device=cuda)
-    _lib.call('pmx_force_vjp', ws.handle, spec, _lib.ptr(T(pmid, cuda)), _lib.ptr(T(disp, cuda)),
-              n, gconf.ptcl_num, 0.3, _lib.ptr(T(cot, cuda)), _lib.ptr(acc), _lib.ptr(dc),
+    _lib.call('pmx_force_vjp', ws.handle, spec, T(pmid, cuda), T(disp, cuda),
+              n, gconf.ptcl_num, 0.3, T(cot, cuda), _lib.ptr(acc), _lib.ptr(dc),
               _lib.ptr(om), _lib.stream_ptr(cuda))
     assert rel_l2(acc.cpu().numpy(), acc_o) < RTOL_ACC
     assert rel_l2(dc.cpu().numpy(), dc_o) < 1e-4

@@ -50,7 +50,7 @@ def enmesh_gpu(dev, dim, wrap, shape, cell, pmid, disp, offset=0, cell_size=None
     ind = torch.empty((n, nk, dim), dtype=torch.int32, device=dev)
     frac = torch.empty((n, nk), dtype=torch.float32, device=dev)
     fg = torch.empty((n, nk, dim), dtype=torch.float32, device=dev)
-    _lib.call('pmx_enmesh', spec, _lib.ptr(T(pmid, dev)), _lib.ptr(T(disp, dev)), n,
+    _lib.call('pmx_enmesh', spec, T(pmid, dev), T(disp, dev), n,
               _lib.ptr(ind), _lib.ptr(frac), _lib.ptr(fg), _lib.stream_ptr(dev))
     torch.cuda.synchronize()
     return ind.cpu().numpy(), frac.cpu().numpy(), fg.cpu().numpy()
@@ -140,7 +140,7 @@ def test_scatter_gather_and_vjps(cuda, case):
     dc = torch.empty((n, dim), dtype=torch.float32, device=cuda)
     vc = torch.empty((n, C), dtype=torch.float32, device=cuda)
     _lib.call('pmx_scatter_adj', spec, _lib.ptr(dP), _lib.ptr(dD), n, _lib.ptr(dV), float(vs), C,
-              _lib.ptr(T(mcot, cuda)), _lib.ptr(dc), _lib.ptr(vc), _lib.stream_ptr(cuda))
+              T(mcot, cuda), _lib.ptr(dc), _lib.ptr(vc), _lib.stream_ptr(cuda))
     assert rel_l2(dc.cpu().numpy(), dc_o) < 1e-5
     assert rel_l2(vc.cpu().numpy().reshape(vc_o.shape), vc_o) < 1e-5
 
@@ -149,7 +149,7 @@ def test_scatter_gather_and_vjps(cuda, case):
     g_o = pm.gather(pmid, disp, conf, mesh0, val=gval, offset=offset, cell_size=cell_size)
     out = torch.empty((n, C), dtype=torch.float32, device=cuda)
     gv = T(gval, cuda) if chan else None
-    _lib.call('pmx_gather', spec, _lib.ptr(dP), _lib.ptr(dD), n, _lib.ptr(T(mesh0, cuda)), C,
+    _lib.call('pmx_gather', spec, _lib.ptr(dP), _lib.ptr(dD), n, T(mesh0, cuda), C,
               _lib.ptr(gv), float(gval) if not chan else 0.0, _lib.ptr(out),
               _lib.stream_ptr(cuda))
     assert rel_l2(out.cpu().numpy().reshape(g_o.shape), g_o) < 1e-6
@@ -160,8 +160,8 @@ def test_scatter_gather_and_vjps(cuda, case):
                                   cell_size=cell_size)
     dc = torch.empty((n, dim), dtype=torch.float32, device=cuda)
     mc = torch.zeros(mesh_shape + chan, dtype=torch.float32, device=cuda)
-    _lib.call('pmx_gather_adj', spec, _lib.ptr(dP), _lib.ptr(dD), n, _lib.ptr(T(mesh0, cuda)), C,
-              _lib.ptr(T(vcot, cuda)), _lib.ptr(dc), _lib.ptr(mc), _lib.stream_ptr(cuda))
+    _lib.call('pmx_gather_adj', spec, _lib.ptr(dP), _lib.ptr(dD), n, T(mesh0, cuda), C,
+              T(vcot, cuda), _lib.ptr(dc), _lib.ptr(mc), _lib.stream_ptr(cuda))
     assert rel_l2(dc.cpu().numpy(), dc_o) < 1e-5
     assert rel_l2(mc.cpu().numpy(), mc_o) < RTOL_MESH
 
@@ -174,7 +174,7 @@ def test_scatter_centered_known_answer(cuda):
         disp = np.tile(np.array(pos, np.float32), (7, 1))
         mesh = torch.zeros((2, 2, 2), dtype=torch.float32, device=cuda)
         spec = _lib.make_spec(3, (2, 2, 2), (2, 2, 2), 2.0)
-        _lib.call('pmx_scatter', spec, _lib.ptr(T(pmid, cuda)), _lib.ptr(T(disp, cuda)), 7, None,
+        _lib.call('pmx_scatter', spec, T(pmid, cuda), T(disp, cuda), 7, None,
                   1.0, 1, _lib.ptr(mesh), _lib.stream_ptr(cuda))
         np.testing.assert_array_equal(mesh.cpu().numpy(), np.full((2, 2, 2), 0.875, np.float32))
 
