@@ -174,6 +174,20 @@ int pmx_drift_adj(float *disp, const float *vel, float *vel_cot,
 int pmx_dot(const float *x, const float *y, int64_t n, double *out,
             void *stream);
 
+/* pmx_dot for callers that cannot let a library allocate device memory
+ * (e.g. a JAX process that preallocated most of the GPU, or a framework
+ * custom call that must not allocate outside its own allocator).  It has no
+ * counterpart in pmwd.  Same result as pmx_dot up to summation order; it
+ * calls no cudaMalloc/cudaFree: its partial sums live in a static 64 KiB
+ * device array that every GPU loading libpmx holds until the process
+ * exits.  n is limited to 2^30 elements (larger n returns PMX_ERR_SHAPE).
+ * The first call on a device looks the array up (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  All calls on a device
+ * share the one array: calls that overlap on the GPU (e.g. on two streams)
+ * race and give wrong sums. */
+int pmx_dot_noalloc(const float *x, const float *y, int64_t n, double *out,
+                    void *stream);
+
 /* One forward step K(1/2) D F K(1/2) of nbody.py:121-140 (``integrate``
  * with the default symp_splits), fused: factors = {K1, D, K2}. */
 int pmx_nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec,

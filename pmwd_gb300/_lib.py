@@ -51,6 +51,7 @@ SIGNATURES = {
     'pmx_kick_adj': (c_int, [c_p, c_p, c_p, c_p, c_p, c_i64, c_f, c_p, c_p]),
     'pmx_drift_adj': (c_int, [c_p, c_p, c_p, c_p, c_i64, c_f, c_p, c_p]),
     'pmx_dot': (c_int, [c_p, c_p, c_i64, c_p, c_p]),
+    'pmx_dot_noalloc': (c_int, [c_p, c_p, c_i64, c_p, c_p]),
     'pmx_nbody_step': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_p, c_p, c_p, c_p, c_i64, c_i64,
                                ctypes.POINTER(c_f), c_d, c_p]),
     'pmx_nbody_adj_step': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_p, c_p, c_p, c_p, c_p, c_p,

@@ -1139,3 +1139,85 @@ extern "C" const char *pmx_profile_stage_name(int i) {
     if (i < 0 || i >= PMX_PROF_STAGES) return nullptr;
     return kStageNames[i];
 }
+
+// ---------------------------------------------------------------------------
+// Dot product that allocates nothing
+//
+// Some callers cannot let a library call cudaMalloc: a JAX/XLA process that
+// has preallocated most of the GPU for its own pool (pmwd's notebooks set
+// XLA_PYTHON_CLIENT_MEM_FRACTION=.95), or a framework custom call that must
+// not allocate outside the framework's allocator.  pmx_dot_noalloc serves
+// them: its per-block partial sums live in the file-scope array below, which
+// the module places in device memory when the library is loaded (64 KiB on
+// every GPU that loads libpmx, held until the process exits).  Host code
+// must not pass the array's name to a kernel -- on the host it is only a
+// stand-in -- so the device address is looked up once per device with
+// cudaGetSymbolAddress and passed as an argument.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr int64_t NOALLOC_CHUNK = int64_t(1) << 17;  // elements summed per block
+constexpr int NOALLOC_BLOCKS = 8192;                 // partial sums the array holds
+
+__device__ __align__(256) double g_noalloc_partials[NOALLOC_BLOCKS];
+
+std::mutex g_noalloc_mu;
+double *g_noalloc_addr[64] = {nullptr};
+
+// Device address of g_noalloc_partials on the current device, looked up at
+// the first call on that device (with that device current).
+int noalloc_partials(double **out) {
+    int dev = 0;
+    PMX_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(PMX_ERR_ARG, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_partials)");
+        g_noalloc_addr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return PMX_OK;
+}
+
+// Block b sums x*y over elements [b*CHUNK, (b+1)*CHUNK) into part[b].
+__global__ void __launch_bounds__(PT) k_dot_chunks(const float *__restrict__ x,
+                                                   const float *__restrict__ y, int64_t n,
+                                                   double *part) {
+    __shared__ double sh[PT / 32];
+    int64_t beg = (int64_t)blockIdx.x * NOALLOC_CHUNK;
+    int64_t end = beg + NOALLOC_CHUNK < n ? beg + NOALLOC_CHUNK : n;
+    double s = 0.0;
+    for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) s += (double)x[i] * (double)y[i];
+    double t = block_sum<PT>(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+}  // namespace
+
+extern "C" int pmx_dot_noalloc(const float *x, const float *y, int64_t n, double *out,
+                               void *stream) {
+    if (n < 0 || !out) return fail(PMX_ERR_ARG, "pmx_dot_noalloc: bad arguments");
+    if (n > NOALLOC_CHUNK * NOALLOC_BLOCKS)
+        return fail(PMX_ERR_SHAPE, "pmx_dot_noalloc: n = " + std::to_string(n) +
+                                       " exceeds its maximum of 2^30 elements (8192 static "
+                                       "partial sums of 2^17 elements each); use pmx_dot");
+    cudaStream_t s = as_stream(stream);
+    if (n == 0) {
+        PMX_CUDA(cudaMemsetAsync(out, 0, sizeof(double), s));
+        return PMX_OK;
+    }
+    if (!x || !y) return fail(PMX_ERR_ARG, "pmx_dot_noalloc: null x/y");
+    double *part = nullptr;
+    int st = noalloc_partials(&part);
+    if (st) return st;
+    int blocks = (int)((n + NOALLOC_CHUNK - 1) / NOALLOC_CHUNK);
+    // every block overwrites its own partial, so no clearing is needed
+    k_dot_chunks<<<blocks, PT, 0, s>>>(x, y, n, part);
+    PMX_LAUNCH_CHECK("k_dot_chunks");
+    k_reduce1<<<1, 1024, 0, s>>>(part, blocks, out);
+    PMX_LAUNCH_CHECK("k_reduce1");
+    return PMX_OK;
+}
