@@ -109,6 +109,9 @@ int pmx_gather_adj(const pmx_enmesh_spec *spec, const int16_t *pmid,
 typedef struct pmx_workspace pmx_workspace;
 
 #define PMX_WS_ADJOINT 1   /* also allocate buffers for the force VJP */
+#define PMX_WS_CUFFT3D 2   /* use 3-D cuFFT plans even where the fused x pass
+                              applies (n0 a power of two in 64..1024);
+                              for comparisons and tests */
 
 /* Device bytes a workspace for this 3-D mesh allocates (meshes, spectra,
  * cuFFT work areas, reduction scratch). */
@@ -206,6 +209,25 @@ int pmx_nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec,
                        float *acc_cot, int64_t n, int64_t ptcl_num,
                        const float factors[3], double omega_m, double *dots,
                        void *stream);
+
+/* pmx_nbody_step / pmx_nbody_adj_step with Kahan-compensated float32 updates
+ * of disp and vel: disp_comp and vel_comp (n, 3) carry the running
+ * compensation terms across steps (zero them at the start of a run).  pmwd
+ * has no counterpart (its updates are plain float32, nbody.py:44,75); this
+ * keeps the rounding of the position/velocity sums from accumulating so the
+ * reverse-time reconstruction of the adjoint returns closer to the initial
+ * state. */
+int pmx_nbody_step_kahan(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                         const int16_t *pmid, float *disp, float *vel, float *acc,
+                         float *disp_comp, float *vel_comp, int64_t n,
+                         int64_t ptcl_num, const float factors[3], double omega_m,
+                         void *stream);
+int pmx_nbody_adj_step_kahan(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                             const int16_t *pmid, float *disp, float *vel, float *acc,
+                             float *disp_cot, float *vel_cot, float *acc_cot,
+                             float *disp_comp, float *vel_comp, int64_t n,
+                             int64_t ptcl_num, const float factors[3],
+                             double omega_m, double *dots, void *stream);
 
 /* --------------------------------------------------------------------------
  * Stage profiler (no counterpart in pmwd, which only times whole jitted

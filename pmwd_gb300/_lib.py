@@ -56,6 +56,11 @@ SIGNATURES = {
                                ctypes.POINTER(c_f), c_d, c_p]),
     'pmx_nbody_adj_step': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_p, c_p, c_p, c_p, c_p, c_p,
                                    c_p, c_i64, c_i64, ctypes.POINTER(c_f), c_d, c_p, c_p]),
+    'pmx_nbody_step_kahan': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_p, c_p, c_p, c_p, c_p,
+                                     c_p, c_i64, c_i64, ctypes.POINTER(c_f), c_d, c_p]),
+    'pmx_nbody_adj_step_kahan': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_p, c_p, c_p, c_p, c_p,
+                                         c_p, c_p, c_p, c_p, c_i64, c_i64, ctypes.POINTER(c_f),
+                                         c_d, c_p, c_p]),
     'pmx_profile_enable': (c_int, [c_p, c_int]),
     'pmx_profile_read': (c_int, [c_p, ctypes.POINTER(c_d), ctypes.POINTER(c_i64),
                                  ctypes.POINTER(c_i64)]),
@@ -78,6 +83,7 @@ def profile_read(ws):
     return out, launches.value
 
 PMX_WS_ADJOINT = 1
+PMX_WS_CUFFT3D = 2
 
 _lib = None
 _lock = threading.Lock()
@@ -153,16 +159,16 @@ def make_spec(dim, wrap_shape, mesh_shape, conf_cell_size, offset=0, cell_size=N
 class Workspace:
     """Owner of a ``pmx_workspace`` (mesh buffers, spectra, cuFFT plans)."""
 
-    def __init__(self, mesh_shape, adjoint=True, device=None):
+    def __init__(self, mesh_shape, adjoint=True, device=None, cufft3d=False):
         load()
         self.mesh_shape = tuple(int(s) for s in mesh_shape)
         self.adjoint = adjoint
+        flags = (PMX_WS_ADJOINT if adjoint else 0) | (PMX_WS_CUFFT3D if cufft3d else 0)
         self.device = torch.device('cuda', torch.cuda.current_device() if device is None else device)
         shp = (c_i64 * 3)(*self.mesh_shape)
         h = c_p()
         with torch.cuda.device(self.device):
-            check(_lib.pmx_workspace_create(shp, PMX_WS_ADJOINT if adjoint else 0,
-                                            ctypes.byref(h)), 'pmx_workspace_create')
+            check(_lib.pmx_workspace_create(shp, flags, ctypes.byref(h)), 'pmx_workspace_create')
         self.handle = h
 
     def __del__(self):

@@ -20,6 +20,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -73,6 +74,13 @@ struct pmx_workspace {
     cufftHandle r2c1 = 0, c2r3 = 0, r2c3 = 0, c2r1 = 0;
     bool have_r2c1 = false, have_c2r3 = false, have_r2c3 = false, have_c2r1 = false;
     double ktab_cell = -1.0;
+    // power-of-two meshes: slab-wise 2-D cuFFT over (y, z) plus the fused
+    // x pass of pmx_fft.cu; meshes are then plane-interleaved (x, 3, n1, n2)
+    bool xfast = false;
+    int64_t slab = 0;           // x-planes per 2-D cuFFT execution
+    float2 *tw = nullptr;       // exp(-2 pi i m / n0)
+    cufftHandle p2r = 0, p2c3 = 0, p2r3 = 0, p2c = 0;  // 2-D r2c, c2r x3, r2c x3, c2r
+    bool have_p2r = false, have_p2c3 = false, have_p2r3 = false, have_p2c = false;
     // stage profiler: CUDA events around every stage while enabled
     bool prof_on = false;
     struct Rec {
@@ -254,6 +262,12 @@ struct Hot {
     int64_t stride[3];
     float cell;   // f32(conf.cell_size), also the disp_cot divisor
     float val;    // f32(mesh_size / ptcl_num)
+    // component j of the acceleration meshes (and their cotangents) at cell
+    // c with x index x lives at c + x*gxs + j*gjs: planar (0, M) or
+    // plane-interleaved (x, 3, n1, n2) = (2 n1 n2, n1 n2)
+    int64_t gxs, gjs;
+    // optional Kahan compensation terms of disp and vel (n, 3); NULL = plain
+    float *dcomp, *vcomp;
 };
 
 __device__ __forceinline__ void hot_axis(const Hot &h, int a, int pm, float d, Axis &ax) {
@@ -290,6 +304,20 @@ __device__ __forceinline__ float3 axmy3(float3 y, float3 x, float a) {  // y - x
     return make_float3(__fsub_rn(y.x, __fmul_rn(x.x, a)), __fsub_rn(y.y, __fmul_rn(x.y, a)),
                        __fsub_rn(y.z, __fmul_rn(x.z, a)));
 }
+// y + x*a with Kahan compensation kept in comp[3q..3q+2] (comp == NULL:
+// the plain float32 update of the reference).
+__device__ __forceinline__ float3 kahan_axpy(float3 y, float3 x, float a, float *comp, int64_t q) {
+    if (!comp) return axpy3(y, x, a);
+    float3 c = ld3(comp, q);
+    float3 u = make_float3(__fsub_rn(__fmul_rn(x.x, a), c.x), __fsub_rn(__fmul_rn(x.y, a), c.y),
+                           __fsub_rn(__fmul_rn(x.z, a), c.z));
+    float3 t = make_float3(__fadd_rn(y.x, u.x), __fadd_rn(y.y, u.y), __fadd_rn(y.z, u.z));
+    c = make_float3(__fsub_rn(__fsub_rn(t.x, y.x), u.x), __fsub_rn(__fsub_rn(t.y, y.y), u.y),
+                    __fsub_rn(__fsub_rn(t.z, y.z), u.z));
+    st3(comp, q, c);
+    return t;
+}
+
 __device__ __forceinline__ double dot3d(float3 a, float3 b) {
     return (double)a.x * (double)b.x + (double)a.y * (double)b.y + (double)a.z * (double)b.z;
 }
@@ -317,8 +345,8 @@ __global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ p
          q += (int64_t)gridDim.x * blockDim.x) {
         float3 d = ld3(disp, q);
         if (KD) {
-            float3 v = axpy3(ld3(vel, q), ld3(acc, q), K1);
-            d = axpy3(d, v, D);
+            float3 v = kahan_axpy(ld3(vel, q), ld3(acc, q), K1, h.vcomp, q);
+            d = kahan_axpy(d, v, D, h.dcomp, q);
             st3(vel, q, v);
             st3(disp, q, d);
         }
@@ -343,13 +371,14 @@ __global__ void __launch_bounds__(PT) k_gather3(Hot h, const int16_t *__restrict
         for (int k = 0; k < 8; ++k) {
             int64_t c = hot_cell(h, ax, k);
             float f = frac_of(ax, k);
-            a0 = __fadd_rn(a0, __fmul_rn(__ldg(g + c), f));
-            a1 = __fadd_rn(a1, __fmul_rn(__ldg(g + M + c), f));
-            a2 = __fadd_rn(a2, __fmul_rn(__ldg(g + 2 * M + c), f));
+            const float *gc = g + c + (int64_t)ax[0].i[k & 1] * h.gxs;
+            a0 = __fadd_rn(a0, __fmul_rn(__ldg(gc), f));
+            a1 = __fadd_rn(a1, __fmul_rn(__ldg(gc + h.gjs), f));
+            a2 = __fadd_rn(a2, __fmul_rn(__ldg(gc + 2 * h.gjs), f));
         }
         float3 a = make_float3(a0, a1, a2);
         st3(acc, q, a);
-        if (KICK) st3(vel, q, axpy3(ld3(vel, q), a, K2));
+        if (KICK) st3(vel, q, kahan_axpy(ld3(vel, q), a, K2, h.vcomp, q));
     }
 }
 
@@ -370,10 +399,10 @@ __global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pm
         if (KD) {
             float3 a = ld3(acc, q);
             float3 vc = ld3(vel_cot, q);
-            float3 v = axpy3(ld3(vel, q), a, K1);
+            float3 v = kahan_axpy(ld3(vel, q), a, K1, h.vcomp, q);
             float3 dc = axmy3(ld3(disp_cot, q), ld3(alpha, q), K1);
             s0 += dot3d(vc, a);
-            d = axpy3(d, v, D);
+            d = kahan_axpy(d, v, D, h.dcomp, q);
             vc = axmy3(vc, dc, D);
             s1 += dot3d(dc, v);
             st3(vel, q, v);
@@ -420,7 +449,8 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
             float f = frac_of(ax, k);
             float fg[3];
             frac_grad_of(ax, k, fg);
-            float m0 = __ldg(g + c), m1 = __ldg(g + M + c), m2 = __ldg(g + 2 * M + c);
+            const int64_t gc = c + (int64_t)ax[0].i[k & 1] * h.gxs;
+            float m0 = __ldg(g + gc), m1 = __ldg(g + gc + h.gjs), m2 = __ldg(g + gc + 2 * h.gjs);
             a0 = __fadd_rn(a0, __fmul_rn(m0, f));
             a1 = __fadd_rn(a1, __fmul_rn(m1, f));
             a2 = __fadd_rn(a2, __fmul_rn(m2, f));
@@ -429,9 +459,9 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
             c0 = __fadd_rn(c0, __fmul_rn(t, fg[0]));
             c1 = __fadd_rn(c1, __fmul_rn(t, fg[1]));
             c2 = __fadd_rn(c2, __fmul_rn(t, fg[2]));
-            atomicAdd(mcot + c, __fmul_rn(vc.x, f));
-            atomicAdd(mcot + M + c, __fmul_rn(vc.y, f));
-            atomicAdd(mcot + 2 * M + c, __fmul_rn(vc.z, f));
+            atomicAdd(mcot + gc, __fmul_rn(vc.x, f));
+            atomicAdd(mcot + gc + h.gjs, __fmul_rn(vc.y, f));
+            atomicAdd(mcot + gc + 2 * h.gjs, __fmul_rn(vc.z, f));
         }
         float3 a = make_float3(a0, a1, a2);
         st3(acc, q, a);
@@ -473,7 +503,7 @@ __global__ void __launch_bounds__(PT) k_sadj(Hot h, const int16_t *__restrict__ 
                          __fadd_rn(al.z, __fdiv_rn(c2, h.cell)));
         st3(alpha, q, al);
         if (KICK) {
-            st3(vel, q, axpy3(ld3(vel, q), ld3(acc, q), K2));
+            st3(vel, q, kahan_axpy(ld3(vel, q), ld3(acc, q), K2, h.vcomp, q));
             st3(disp_cot, q, axmy3(ld3(disp_cot, q), al, K2));
         }
     }
@@ -614,6 +644,15 @@ int check_hot(pmx_workspace *ws, const pmx_enmesh_spec *spec, const void *pmid, 
     h->stride[0] = ws->n1 * ws->n2;
     h->cell = (float)spec->conf_cell_size;
     h->val = (float)((double)ws->M / (double)ptcl_num);
+    h->dcomp = nullptr;
+    h->vcomp = nullptr;
+    if (ws->xfast) {
+        h->gxs = 2 * ws->n1 * ws->n2;
+        h->gjs = ws->n1 * ws->n2;
+    } else {
+        h->gxs = 0;
+        h->gjs = ws->M;
+    }
     return PMX_OK;
 }
 
@@ -643,6 +682,30 @@ int poisson_grid(pmx_workspace *ws) {
 int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t st) {
     float s = (float)(1.5 * (double)(float)omega_m);
     float c = (float)((double)s / (double)ws->M);
+    if (ws->xfast) {
+        const int64_t pr = ws->n1 * ws->n2, pc = ws->n1 * ws->n2h, S = ws->slab;
+        float2 *H = reinterpret_cast<float2 *>(ws->g);  // g is free until the c2r
+        {
+            Stage sg(ws, 2, st, 0);
+            PMX_CUFFT(cufftSetStream(ws->p2r, st));
+            for (int64_t x = 0; x < ws->n0; x += S)
+                PMX_CUFFT(cufftExecR2C(ws->p2r, ws->dens + x * pr,
+                                       reinterpret_cast<cufftComplex *>(H + x * pc)));
+        }
+        {
+            Stage sg(ws, 3, st, 1);
+            int st2 = xpass(false, H, ws->ck, ws->ktab, ws->tw, ws->n0, ws->n1, ws->n2h, c, st);
+            if (st2) return st2;
+        }
+        {
+            Stage sg(ws, 4, st, 0);
+            PMX_CUFFT(cufftSetStream(ws->p2c3, st));
+            for (int64_t x = 0; x < ws->n0; x += S)
+                PMX_CUFFT(cufftExecC2R(ws->p2c3, reinterpret_cast<cufftComplex *>(ws->ck + 3 * x * pc),
+                                       ws->g + 3 * x * pr));
+        }
+        return PMX_OK;
+    }
     {
         Stage sg(ws, 2, st, 0);
         PMX_CUFFT(cufftSetStream(ws->r2c1, st));
@@ -662,11 +725,36 @@ int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t s
     return PMX_OK;
 }
 
-// The force VJP tail after k_g3adj has filled ws->mcot: batched r2c, adjoint
-// Fourier kernel, c2r into ws->dens (now rho_cot, scale folded in).
+// The force VJP tail after k_g3adj has filled ws->mcot: r2c of the three
+// cotangent meshes, adjoint Fourier operator, c2r into ws->dens (then
+// rho_cot, scale folded in).
 int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
     float s = (float)(1.5 * (double)(float)omega_m);
     float c = (float)((double)s / (double)ws->M);
+    if (ws->xfast) {
+        const int64_t pr = ws->n1 * ws->n2, pc = ws->n1 * ws->n2h, S = ws->slab;
+        float2 *Sk = reinterpret_cast<float2 *>(ws->g);  // g is dead after k_g3adj
+        {
+            Stage sg(ws, 8, st, 0);
+            PMX_CUFFT(cufftSetStream(ws->p2r3, st));
+            for (int64_t x = 0; x < ws->n0; x += S)
+                PMX_CUFFT(cufftExecR2C(ws->p2r3, ws->mcot + 3 * x * pr,
+                                       reinterpret_cast<cufftComplex *>(ws->ck + 3 * x * pc)));
+        }
+        {
+            Stage sg(ws, 9, st, 1);
+            int st2 = xpass(true, ws->ck, Sk, ws->ktab, ws->tw, ws->n0, ws->n1, ws->n2h, c, st);
+            if (st2) return st2;
+        }
+        {
+            Stage sg(ws, 10, st, 0);
+            PMX_CUFFT(cufftSetStream(ws->p2c, st));
+            for (int64_t x = 0; x < ws->n0; x += S)
+                PMX_CUFFT(cufftExecC2R(ws->p2c, reinterpret_cast<cufftComplex *>(Sk + x * pc),
+                                       ws->dens + x * pr));
+        }
+        return PMX_OK;
+    }
     {
         Stage sg(ws, 8, st, 0);
         PMX_CUFFT(cufftSetStream(ws->r2c3, st));
@@ -702,12 +790,46 @@ int make_plan(cufftHandle *plan, const int64_t shape[3], cufftType type, int64_t
     return PMX_OK;
 }
 
+int make_plan2d(cufftHandle *plan, int64_t n1, int64_t n2, cufftType type, int64_t batch,
+                size_t *work) {
+    PMX_CUFFT(cufftCreate(plan));
+    PMX_CUFFT(cufftSetAutoAllocation(*plan, 0));
+    long long n[2] = {n1, n2};
+    size_t w = 0;
+    PMX_CUFFT(cufftMakePlanMany64(*plan, 2, n, nullptr, 1, 0, nullptr, 1, 0, type, batch, &w));
+    *work = w;
+    return PMX_OK;
+}
+
+// x-planes per 2-D cuFFT execution: PMX_SLAB if set, else the largest power
+// of two dividing n0 whose three-component slab (real + complex planes)
+// stays within 64 MB, so each slab's intermediate stays in L2.
+int64_t choose_slab(int64_t n0, int64_t n1, int64_t n2) {
+    const char *env = std::getenv("PMX_SLAB");
+    int64_t S = 0;
+    if (env) S = std::atoll(env);
+    if (S <= 0) {
+        double plane = (double)n1 * n2 * 4 + (double)n1 * (n2 / 2 + 1) * 8;
+        S = 1;
+        while (S * 2 <= n0 && 3.0 * (S * 2) * plane <= 64.0 * (1 << 20)) S *= 2;
+    }
+    while (S > 1 && n0 % S) S /= 2;
+    if (S < 1) S = 1;
+    if (S > n0) S = n0;
+    return S;
+}
+
 void ws_free(pmx_workspace *ws) {
     if (!ws) return;
     if (ws->have_r2c1) cufftDestroy(ws->r2c1);
     if (ws->have_c2r3) cufftDestroy(ws->c2r3);
     if (ws->have_r2c3) cufftDestroy(ws->r2c3);
     if (ws->have_c2r1) cufftDestroy(ws->c2r1);
+    if (ws->have_p2r) cufftDestroy(ws->p2r);
+    if (ws->have_p2c3) cufftDestroy(ws->p2c3);
+    if (ws->have_p2r3) cufftDestroy(ws->p2r3);
+    if (ws->have_p2c) cufftDestroy(ws->p2c);
+    cudaFree(ws->tw);
     cudaFree(ws->dens);
     cudaFree(ws->ck);
     cudaFree(ws->g);
@@ -791,29 +913,57 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
         ws_free(ws);
         return st;
     }
-    size_t w1 = 0, w2 = 0, w3 = 0, w4 = 0;
-    int64_t shp[3] = {ws->n0, ws->n1, ws->n2};
-    if ((st = make_plan(&ws->r2c1, shp, CUFFT_R2C, 1, &w1))) { ws_free(ws); return st; }
-    ws->have_r2c1 = true;
-    if ((st = make_plan(&ws->c2r3, shp, CUFFT_C2R, 3, &w2))) { ws_free(ws); return st; }
-    ws->have_c2r3 = true;
-    if (flags & PMX_WS_ADJOINT) {
-        if ((st = make_plan(&ws->r2c3, shp, CUFFT_R2C, 3, &w3))) { ws_free(ws); return st; }
-        ws->have_r2c3 = true;
-        if ((st = make_plan(&ws->c2r1, shp, CUFFT_C2R, 1, &w4))) { ws_free(ws); return st; }
-        ws->have_c2r1 = true;
+    const char *xenv = std::getenv("PMX_XFAST");
+    ws->xfast = xpass_supported(ws->n0) && !(flags & PMX_WS_CUFFT3D) && !(xenv && xenv[0] == '0');
+    size_t wk[4] = {0, 0, 0, 0};
+    cufftHandle *ph[4];
+    bool *hv[4];
+    if (ws->xfast) {
+        ws->slab = choose_slab(ws->n0, ws->n1, ws->n2);
+        const int64_t S = ws->slab;
+        if ((st = make_plan2d(&ws->p2r, ws->n1, ws->n2, CUFFT_R2C, S, &wk[0]))) { ws_free(ws); return st; }
+        ws->have_p2r = true;
+        if ((st = make_plan2d(&ws->p2c3, ws->n1, ws->n2, CUFFT_C2R, 3 * S, &wk[1]))) { ws_free(ws); return st; }
+        ws->have_p2c3 = true;
+        if (flags & PMX_WS_ADJOINT) {
+            if ((st = make_plan2d(&ws->p2r3, ws->n1, ws->n2, CUFFT_R2C, 3 * S, &wk[2]))) { ws_free(ws); return st; }
+            ws->have_p2r3 = true;
+            if ((st = make_plan2d(&ws->p2c, ws->n1, ws->n2, CUFFT_C2R, S, &wk[3]))) { ws_free(ws); return st; }
+            ws->have_p2c = true;
+        }
+        std::vector<float2> tw(ws->n0);
+        xpass_twiddles(ws->n0, tw.data());
+        if ((st = alloc((void **)&ws->tw, ws->n0 * sizeof(float2)))) { ws_free(ws); return st; }
+        if (cudaMemcpy(ws->tw, tw.data(), ws->n0 * sizeof(float2), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+            ws_free(ws);
+            return fail(PMX_ERR_CUDA, "twiddle upload failed");
+        }
+        ph[0] = &ws->p2r; ph[1] = &ws->p2c3; ph[2] = &ws->p2r3; ph[3] = &ws->p2c;
+        hv[0] = &ws->have_p2r; hv[1] = &ws->have_p2c3; hv[2] = &ws->have_p2r3; hv[3] = &ws->have_p2c;
+    } else {
+        int64_t shp[3] = {ws->n0, ws->n1, ws->n2};
+        if ((st = make_plan(&ws->r2c1, shp, CUFFT_R2C, 1, &wk[0]))) { ws_free(ws); return st; }
+        ws->have_r2c1 = true;
+        if ((st = make_plan(&ws->c2r3, shp, CUFFT_C2R, 3, &wk[1]))) { ws_free(ws); return st; }
+        ws->have_c2r3 = true;
+        if (flags & PMX_WS_ADJOINT) {
+            if ((st = make_plan(&ws->r2c3, shp, CUFFT_R2C, 3, &wk[2]))) { ws_free(ws); return st; }
+            ws->have_r2c3 = true;
+            if ((st = make_plan(&ws->c2r1, shp, CUFFT_C2R, 1, &wk[3]))) { ws_free(ws); return st; }
+            ws->have_c2r1 = true;
+        }
+        ph[0] = &ws->r2c1; ph[1] = &ws->c2r3; ph[2] = &ws->r2c3; ph[3] = &ws->c2r1;
+        hv[0] = &ws->have_r2c1; hv[1] = &ws->have_c2r3; hv[2] = &ws->have_r2c3; hv[3] = &ws->have_c2r1;
     }
-    size_t wmax = w1;
-    if (w2 > wmax) wmax = w2;
-    if (w3 > wmax) wmax = w3;
-    if (w4 > wmax) wmax = w4;
+    size_t wmax = 0;
+    for (int i = 0; i < 4; ++i)
+        if (wk[i] > wmax) wmax = wk[i];
     if (wmax > 0 && (st = alloc(&ws->fft_work, wmax))) { ws_free(ws); return st; }
     ws->fft_work_bytes = wmax;
-    cufftHandle plans[4] = {ws->r2c1, ws->c2r3, ws->r2c3, ws->c2r1};
-    bool have[4] = {ws->have_r2c1, ws->have_c2r3, ws->have_r2c3, ws->have_c2r1};
     for (int i = 0; i < 4; ++i) {
-        if (!have[i]) continue;
-        cufftResult r = cufftSetWorkArea(plans[i], ws->fft_work);
+        if (!*hv[i]) continue;
+        cufftResult r = cufftSetWorkArea(*ph[i], ws->fft_work);
         if (r != CUFFT_SUCCESS) {
             ws_free(ws);
             return fail(PMX_ERR_CUFFT, std::string("cufftSetWorkArea: ") + cufft_name(r));
@@ -1012,12 +1162,15 @@ extern "C" int pmx_dot(const float *x, const float *y, int64_t n, double *out, v
     return PMX_OK;
 }
 
-extern "C" int pmx_nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int16_t *pmid,
-                              float *disp, float *vel, float *acc, int64_t n, int64_t ptcl_num,
-                              const float factors[3], double omega_m, void *stream) {
+static int nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int16_t *pmid,
+                      float *disp, float *vel, float *acc, int64_t n, int64_t ptcl_num,
+                      const float factors[3], double omega_m, float *dcomp, float *vcomp,
+                      void *stream) {
     Hot h;
     int st = check_hot(ws, spec, pmid, disp, n, ptcl_num, &h);
     if (st) return st;
+    h.dcomp = dcomp;
+    h.vcomp = vcomp;
     if (!factors) return fail(PMX_ERR_ARG, "null factors");
     if (n > 0 && (!vel || !acc)) return fail(PMX_ERR_ARG, "null vel/acc");
     cudaStream_t s = as_stream(stream);
@@ -1046,14 +1199,16 @@ extern "C" int pmx_nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, co
     return PMX_OK;
 }
 
-extern "C" int pmx_nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec,
-                                  const int16_t *pmid, float *disp, float *vel, float *acc,
-                                  float *disp_cot, float *vel_cot, float *acc_cot, int64_t n,
-                                  int64_t ptcl_num, const float factors[3], double omega_m,
-                                  double *dots, void *stream) {
+static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int16_t *pmid,
+                          float *disp, float *vel, float *acc, float *disp_cot, float *vel_cot,
+                          float *acc_cot, int64_t n, int64_t ptcl_num, const float factors[3],
+                          double omega_m, double *dots, float *dcomp, float *vcomp,
+                          void *stream) {
     Hot h;
     int st = check_hot(ws, spec, pmid, disp, n, ptcl_num, &h);
     if (st) return st;
+    h.dcomp = dcomp;
+    h.vcomp = vcomp;
     if (!(ws->flags & PMX_WS_ADJOINT)) return fail(PMX_ERR_ARG, "workspace lacks PMX_WS_ADJOINT");
     if (!factors || !dots) return fail(PMX_ERR_ARG, "null factors/dots");
     if (n > 0 && (!vel || !acc || !disp_cot || !vel_cot || !acc_cot))
@@ -1098,6 +1253,43 @@ extern "C" int pmx_nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec
         PMX_LAUNCH_CHECK("k_finish");
     }
     return PMX_OK;
+}
+
+extern "C" int pmx_nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int16_t *pmid,
+                              float *disp, float *vel, float *acc, int64_t n, int64_t ptcl_num,
+                              const float factors[3], double omega_m, void *stream) {
+    return nbody_step(ws, spec, pmid, disp, vel, acc, n, ptcl_num, factors, omega_m, nullptr,
+                      nullptr, stream);
+}
+
+extern "C" int pmx_nbody_step_kahan(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                                    const int16_t *pmid, float *disp, float *vel, float *acc,
+                                    float *disp_comp, float *vel_comp, int64_t n,
+                                    int64_t ptcl_num, const float factors[3], double omega_m,
+                                    void *stream) {
+    if (n > 0 && (!disp_comp || !vel_comp)) return fail(PMX_ERR_ARG, "null compensation arrays");
+    return nbody_step(ws, spec, pmid, disp, vel, acc, n, ptcl_num, factors, omega_m, disp_comp,
+                      vel_comp, stream);
+}
+
+extern "C" int pmx_nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                                  const int16_t *pmid, float *disp, float *vel, float *acc,
+                                  float *disp_cot, float *vel_cot, float *acc_cot, int64_t n,
+                                  int64_t ptcl_num, const float factors[3], double omega_m,
+                                  double *dots, void *stream) {
+    return nbody_adj_step(ws, spec, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n, ptcl_num,
+                          factors, omega_m, dots, nullptr, nullptr, stream);
+}
+
+extern "C" int pmx_nbody_adj_step_kahan(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                                        const int16_t *pmid, float *disp, float *vel, float *acc,
+                                        float *disp_cot, float *vel_cot, float *acc_cot,
+                                        float *disp_comp, float *vel_comp, int64_t n,
+                                        int64_t ptcl_num, const float factors[3],
+                                        double omega_m, double *dots, void *stream) {
+    if (n > 0 && (!disp_comp || !vel_comp)) return fail(PMX_ERR_ARG, "null compensation arrays");
+    return nbody_adj_step(ws, spec, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n, ptcl_num,
+                          factors, omega_m, dots, disp_comp, vel_comp, stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -72,6 +72,15 @@ struct EmParams {
 
 int make_em_params(const pmx_enmesh_spec *spec, EmParams *p);
 
+// Fused x-axis pass of the Poisson solve (pmx_fft.cu).  Forward (adj =
+// false): in = FFT_yz(rho) (n0, n1, n2h), out = the three gradient spectra
+// (n0, 3, n1, n2h) after the inverse x transform.  Adjoint: in = FFT_yz of
+// the three mesh cotangents (n0, 3, n1, n2h), out = (n0, n1, n2h).
+bool xpass_supported(int64_t n0);
+int xpass(bool adj, const float2 *in, float2 *out, const float *kt, const float2 *tw, int64_t n0,
+          int64_t n1, int64_t n2h, float c, cudaStream_t st);
+void xpass_twiddles(int64_t n, float2 *host);
+
 __device__ __forceinline__ int pymod(int x, int m) {
     int r = x % m;
     return r < 0 ? r + m : r;

@@ -49,6 +49,60 @@ def test_force_matches_oracle(cuda, ptcl, mesh, spacing):
     assert rel_l2(acc.cpu().numpy(), acc_o) < RTOL_ACC
 
 
+XPASS_CASES = [((32, 32, 32), 2, 1.0), ((32, 16, 24), 4, 2.0), ((64, 64, 64), 1, 2.0),
+               ((128, 64, 32), 1, 1.0), ((128, 128, 128), 2, 2.0)]
+
+
+def _force_both_paths(cuda, gconf, pmid, disp, cot=None):
+    """pmx_force / pmx_force_vjp on a fused-x-pass workspace and on a 3-D
+    cuFFT workspace."""
+    out = []
+    for cufft3d in (False, True):
+        ws = _lib.Workspace(gconf.mesh_shape, adjoint=True, cufft3d=cufft3d)
+        spec = _lib.make_spec(3, gconf.mesh_shape, gconf.mesh_shape, gconf.cell_size)
+        n = len(pmid)
+        P, D = T(pmid, cuda), T(disp, cuda)
+        acc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+        if cot is None:
+            _lib.call('pmx_force', ws.handle, spec, P, D, n, gconf.ptcl_num, 0.3, acc,
+                      _lib.stream_ptr(cuda))
+            out.append(acc.cpu().numpy())
+        else:
+            dc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+            om = torch.zeros((), dtype=torch.float64, device=cuda)
+            _lib.call('pmx_force_vjp', ws.handle, spec, P, D, n, gconf.ptcl_num, 0.3,
+                      T(cot, cuda), acc, dc, om, _lib.stream_ptr(cuda))
+            out.append((acc.cpu().numpy(), dc.cpu().numpy(), float(om)))
+        del ws
+    return out
+
+
+@pytest.mark.parametrize('ptcl, mesh, spacing', XPASS_CASES)
+def test_fused_xpass_force_matches_oracle(cuda, ptcl, mesh, spacing):
+    """Power-of-two n0 (64..1024) takes the slab 2-D cuFFT + fused x-pass
+    path; it must match the oracle and the 3-D cuFFT path."""
+    oconf, gconf, pmid, disp, vel = make(ptcl, mesh, spacing, 1.5 * spacing)
+    acc_o = pm.gravity(pmid, disp, 0.3, oconf)
+    fast, ref3d = _force_both_paths(cuda, gconf, pmid, disp)
+    assert rel_l2(fast, acc_o) < RTOL_ACC
+    assert rel_l2(ref3d, acc_o) < RTOL_ACC
+    assert rel_l2(fast, ref3d) < RTOL_ACC
+
+
+@pytest.mark.parametrize('ptcl, mesh, spacing', XPASS_CASES[:3])
+def test_fused_xpass_force_vjp_matches_oracle(cuda, ptcl, mesh, spacing):
+    oconf, gconf, pmid, disp, vel = make(ptcl, mesh, spacing, 1.5 * spacing)
+    cot = np.random.default_rng(12).normal(size=disp.shape).astype(np.float32)
+    oconf64 = oc.OConf(spacing, ptcl, mesh, float_dtype=np.float64)
+    acc_o, dc_o, om_o = pm.gravity_vjp(pmid, disp.astype(np.float64), 0.3, oconf64,
+                                       cot.astype(np.float64))
+    (a_f, dc_f, om_f), (a_3, dc_3, om_3) = _force_both_paths(cuda, gconf, pmid, disp, cot)
+    for a, dc, om in ((a_f, dc_f, om_f), (a_3, dc_3, om_3)):
+        assert rel_l2(a, acc_o) < RTOL_ACC
+        assert rel_l2(dc, dc_o) < 1e-4
+        assert abs(om / om_o - 1) < 1e-4
+
+
 @pytest.mark.parametrize('ptcl, mesh', [((16, 16, 16), 2), ((10, 12, 14), 1)])
 def test_force_vjp_matches_oracle(cuda, ptcl, mesh):
     oconf, gconf, pmid, disp, vel = make(ptcl, mesh, 2.0, 2.0)
@@ -94,9 +148,10 @@ def _run_gpu_nbody(gconf, pmid, disp, vel, cosmo, dev):
     return out
 
 
-@pytest.fixture(scope='module')
-def nb_case():
-    oconf, gconf, pmid, disp, vel = make((16, 16, 16), 2, 4.0, 0.5, a_step=1 / 8)
+@pytest.fixture(scope='module', params=[(16, 2), (32, 2)], ids=['32mesh', '64mesh_xpass'])
+def nb_case(request):
+    side, ratio = request.param
+    oconf, gconf, pmid, disp, vel = make((side,) * 3, ratio, 4.0, 0.5, a_step=1 / 8)
     ocos = oc.with_tables(oc.simple_lcdm(), oconf)
     gcos = pg.boltzmann(pg.SimpleLCDM(gconf), gconf)
     return oconf, gconf, pmid, disp, vel, ocos, gcos
@@ -180,3 +235,29 @@ def test_nbody_adjoint_matches_oracle(cuda, nb_case):
     assert abs(float(omg) / sens['Omega_m'] - 1) < 1e-3
     # the reconstructed initial state returns to the start
     assert rel_l2(p0.disp.cpu().numpy(), disp) < 1e-4
+
+
+def test_reversibility_plain_and_kahan(cuda):
+    """Forward to a=1 then reverse=True back to a_start returns to the 2LPT
+    state (docs/examples/adjoint.ipynb, 'Reversibility'); the compensated
+    (Kahan) updates keep the float32 rounding of the disp/vel sums from
+    accumulating.  Stated bound: relative RMS error of disp and vel <= 2e-3
+    for 32^3 particles, 64^3 mesh, 32 steps."""
+    conf = pg.Configuration(4.0, (32, 32, 32), 2, a_nbody_maxstep=(1 - 1 / 64) / 32)
+    cosmo = pg.boltzmann(pg.SimpleLCDM(conf), conf)
+    with torch.no_grad():
+        modes = pg.linear_modes(pg.white_noise(0, conf, device=cuda), cosmo, conf)
+        p0, _ = pg.lpt(modes, cosmo, conf)
+    errs = {}
+    for kahan in (False, True):
+        c = conf.replace(kahan=kahan)
+        with torch.no_grad():
+            p1, _ = pg.nbody(p0, None, cosmo, c)
+            p2, _ = pg.nbody(p1, None, cosmo, c, reverse=True)
+        ed = float((p2.disp - p0.disp).double().std() / p0.disp.double().std())
+        ev = float((p2.vel - p0.vel).double().std() / p0.vel.double().std())
+        errs[kahan] = (ed, ev)
+    print('reversibility (disp, vel) plain', errs[False], 'kahan', errs[True])
+    for ed, ev in errs.values():
+        assert ed < 2e-3 and ev < 2e-3
+    assert errs[True][0] <= 1.5 * errs[False][0] + 1e-7

@@ -1,0 +1,72 @@
+"""GPU initial conditions and analysis against the oracle: linear modes,
+2LPT displacements/velocities (lpt.py:136-212) and the power spectrum
+(spec_util.py:50-147); plus the published LPT statistics of the reference's
+quickstart notebook as a statistical pin."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cosmo as oc, ics
+import pmwd_gb300 as pg
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.fixture(scope='module')
+def ic_case():
+    oconf = oc.OConf(4.0, (32, 32, 32), 2, float_dtype=np.float32)
+    gconf = pg.Configuration(4.0, (32, 32, 32), 2)
+    ocos = oc.with_tables(oc.simple_lcdm(), oconf)
+    gcos = pg.boltzmann(pg.SimpleLCDM(gconf), gconf)
+    noise = np.random.default_rng(0).standard_normal((32, 32, 32), dtype=np.float32)
+    return oconf, gconf, ocos, gcos, noise
+
+
+def test_linear_modes_and_lpt_match_oracle(cuda, ic_case):
+    oconf, gconf, ocos, gcos, noise = ic_case
+    m_o = ics.linear_modes(noise, ocos, oconf)
+    m_g = pg.linear_modes(torch.from_numpy(noise).to(cuda), gcos, gconf)
+    assert rel_l2(m_g.cpu().numpy(), m_o) < 1e-5
+    pmid_o, disp_o, vel_o = ics.lpt(m_o, ocos, oconf)
+    ptcl, obs = pg.lpt(m_g, gcos, gconf)
+    assert obs is None
+    np.testing.assert_array_equal(ptcl.pmid.cpu().numpy(), pmid_o)
+    grid = ics.gen_grid(oconf)[1]
+    assert rel_l2(ptcl.disp.cpu().numpy() - grid, disp_o - grid) < 1e-4
+    assert rel_l2(ptcl.vel.cpu().numpy(), vel_o) < 1e-4
+
+
+def test_powspec_matches_oracle(cuda, ic_case):
+    oconf, gconf, ocos, gcos, noise = ic_case
+    f = np.random.default_rng(3).normal(size=(32, 32, 32)).astype(np.float32)
+    k_o, P_o, N_o, b_o = ics.powspec(f, 2.0)
+    from pmwd_gb300.spec_util import powspec
+    k_g, P_g, N_g, b_g = powspec(torch.from_numpy(f).to(cuda), 2.0)
+    np.testing.assert_allclose(N_g.cpu().numpy(), N_o)
+    np.testing.assert_allclose(k_g.cpu().numpy(), k_o, rtol=1e-12)
+    np.testing.assert_allclose(P_g.cpu().numpy(), P_o, rtol=1e-5)
+    np.testing.assert_allclose(b_g.cpu().numpy(), b_o, rtol=1e-12)
+
+
+def test_lpt_statistics_match_published(cuda):
+    """docs/examples/quickstart.ipynb prints, for 256^3 particles, spacing 1,
+    2x mesh, SimpleLCDM, after 2LPT at a=1/64: disp.std() = 0.105 and
+    vel.std() = 0.007 (3 digits).  Our white noise is a different
+    realisation of the same distribution, so agreement is statistical (a few
+    percent: the large-scale modes of a 256 Mpc/h box carry cosmic variance)."""
+    conf = pg.Configuration(1.0, (256, 256, 256), 2)
+    cosmo = pg.boltzmann(pg.SimpleLCDM(conf), conf)
+    with torch.no_grad():
+        modes = pg.linear_modes(pg.white_noise(0, conf, device=cuda), cosmo, conf)
+        ptcl, _ = pg.lpt(modes, cosmo, conf)
+    disp_std = float(ptcl.disp.double().std())
+    vel_std = float(ptcl.vel.double().std())
+    assert abs(disp_std / 0.105 - 1) < 0.05, disp_std
+    assert abs(vel_std / 0.007 - 1) < 0.08, vel_std   # printed to one significant digit

@@ -1,0 +1,106 @@
+"""Host-side float64 logic of pmwd_gb300 against the oracle: configuration
+derived fields, background functions, growth tables and their parameter
+Jacobian, transfer function, time-step factors and the op schedules."""
+
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cosmo as oc, nbody as onb
+import pmwd_gb300 as pg
+
+gnb = importlib.import_module('pmwd_gb300.nbody')
+
+
+@pytest.fixture(scope='module')
+def both():
+    oconf = oc.OConf(2.0, (16, 16, 16), 2, a_nbody_maxstep=1 / 16)
+    gconf = pg.Configuration(2.0, (16, 16, 16), 2, a_nbody_maxstep=1 / 16)
+    ocos = oc.with_tables(oc.simple_lcdm(), oconf)
+    gcos = pg.boltzmann(pg.SimpleLCDM(gconf), gconf)
+    return oconf, gconf, ocos, gcos
+
+
+def test_configuration_fields(both):
+    oconf, gconf, _, _ = both
+    assert gconf.mesh_shape == (32, 32, 32)
+    assert gconf.cell_size == oconf.cell_size == 1.0
+    np.testing.assert_array_equal(gconf.a_nbody.numpy(), oconf.a_nbody)
+    np.testing.assert_array_equal(gconf.growth_a.numpy(), oconf.growth_a)
+    np.testing.assert_array_equal(gconf.transfer_k.numpy(), oconf.transfer_k)
+    assert gconf.a_nbody_num == 16
+    assert pg.Configuration(1.0, (8, 8, 8)).a_nbody_num == 63   # the reference's default
+    with pytest.raises(ValueError):
+        pg.Configuration(1.0, (8, 8, 8), (8, 8, 4))
+    with pytest.raises(ValueError):
+        pg.Configuration(1.0, (8, 8, 8), 0.5)
+    with pytest.raises(ValueError):
+        pg.Configuration(1.0, (8, 8, 8), symp_splits=((0, 0.5), (1, 0.4)))
+
+
+def test_background_and_tables(both):
+    oconf, gconf, ocos, gcos = both
+    a = torch.linspace(0.01, 1.0, 50, dtype=torch.float64)
+    np.testing.assert_allclose(pg.E2(a, gcos).numpy(), oc.E2(a.numpy(), ocos), rtol=1e-14)
+    np.testing.assert_allclose(pg.H_deriv(a, gcos).numpy(), oc.H_deriv(a.numpy(), ocos),
+                               rtol=1e-12)
+    np.testing.assert_allclose(gcos.growth.numpy(), ocos.growth, rtol=2e-8, atol=1e-12)
+    np.testing.assert_allclose(gcos.transfer.numpy(), ocos.transfer, rtol=1e-12)
+    k = torch.logspace(-3, 1, 40, dtype=torch.float64)
+    np.testing.assert_allclose(pg.linear_power(k, 0.5, gcos, gconf).numpy(),
+                               oc.linear_power(k.numpy(), 0.5, ocos, oconf), rtol=1e-7)
+    np.testing.assert_allclose(float(gcos.sigma8), np.sqrt(oc.sigma2_tophat(8.0, ocos, oconf, 1.0)),
+                               rtol=2e-4)
+
+
+def test_growth_jacobian_matches_finite_differences(both):
+    _, gconf, _, _ = both
+    Om = torch.tensor(0.3, dtype=torch.float64, requires_grad=True)
+    cos = pg.SimpleLCDM(gconf).replace(Omega_m=Om)
+    cos = pg.boltzmann(cos, gconf, transfer=False, varlin=False)
+    w = torch.randn(cos.growth.shape, dtype=torch.float64, generator=torch.Generator().manual_seed(0))
+    (cos.growth * w).sum().backward()
+    h = 1e-5
+    vals = []
+    for s in (1, -1):
+        c = oc.OConf(2.0, (16, 16, 16), 2, a_nbody_maxstep=1 / 16)
+        vals.append((oc.growth_table(oc.simple_lcdm(Omega_m=0.3 + s * h), c) * w.numpy()).sum())
+    np.testing.assert_allclose(float(Om.grad), (vals[0] - vals[1]) / (2 * h), rtol=1e-5)
+
+
+@pytest.mark.parametrize('reverse', [False, True])
+def test_factors_and_schedules(both, reverse):
+    oconf, gconf, ocos, gcos = both
+    log = []
+    # the oracle's own op order for the forward run
+    st = onb.State(np.zeros((1, 3), np.int16), np.zeros((1, 3), np.float32),
+                   np.zeros((1, 3), np.float32), np.zeros((1, 3), np.float32))
+    a = oconf.a_nbody[::-1] if reverse else oconf.a_nbody
+    for a_prev, a_next in zip(a[:-1], a[1:]):
+        onb.kick(a_prev, a_prev, a_prev * 0.5 + a_next * 0.5, st, ocos, oconf, log)
+        onb.drift(a_prev * 0.5 + a_next * 0.5, a_prev, a_next, st, ocos, oconf, log)
+        onb.kick(a_next, a_prev * 0.5 + a_next * 0.5, a_next, st, ocos, oconf, log)
+    ops = gnb.forward_ops(gconf, reverse)
+    f = gnb.op_factors(ops, gcos, gconf).detach().numpy()
+    np.testing.assert_allclose(f, [x[2] for x in log], rtol=1e-8)
+    assert [o[0] for o in ops if o[0] != 'force'] == [x[0] for x in log]
+
+
+def test_factor_gradient_wrt_cosmology(both):
+    """d(kick factor)/d(Omega_m) by autograd through the growth Jacobian vs
+    central differences of the oracle's factor."""
+    oconf, gconf, _, _ = both
+    Om = torch.tensor(0.3, dtype=torch.float64, requires_grad=True)
+    cos = pg.boltzmann(pg.SimpleLCDM(gconf).replace(Omega_m=Om), gconf, transfer=False,
+                       varlin=False)
+    args = (0.25, 0.25, 0.3)
+    K = gnb.kick_factor(*args, cos, gconf)
+    K.backward()
+    h = 1e-5
+    fd = []
+    for s in (1, -1):
+        c = oc.with_tables(oc.simple_lcdm(Omega_m=0.3 + s * h), oconf)
+        fd.append(oc.kick_factor(*args, c, oconf))
+    np.testing.assert_allclose(float(Om.grad), (fd[0] - fd[1]) / (2 * h), rtol=1e-5)
