@@ -174,6 +174,23 @@ def ncu_traffic():
     return out
 
 
+def replica_throughput(ms_local, units_local, world, device):
+    """Whole-job throughput of independent replicas: the slowest rank's time
+    (max over ranks) and the units (particle-steps) all ranks processed.
+    No data-path collective: this reduction happens once, after timing."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms_local, float(units_local)], dtype=torch.float64, device=device)
+    if world > 1:
+        mx = t[:1].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        tot = t[1:].clone()
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        t = torch.cat((mx, tot))
+    ms = float(t[0])
+    return ms, float(t[1]) / (ms / 1e3)
+
+
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle (CPU restatement of the reference algorithm)
 # ---------------------------------------------------------------------------
@@ -321,12 +338,8 @@ def run_pmx(args, rank, world, local_rank):
     clk = clocks.stop()
     ms_total = e0.elapsed_time(e1)
     stages, launches = _lib.profile_read(ws)
-    t = torch.tensor([ms_total], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_total = float(t)
+    ms_total, value = replica_throughput(ms_total, N * args.steps, world, dev)
     ms_step = ms_total / args.steps
-    value = world * N * args.steps / (ms_total / 1e3)
 
     # ---- e2e: the same step pair through the C ABI with host buffers ----
     e2e = None

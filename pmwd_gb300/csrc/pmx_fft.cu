@@ -259,14 +259,28 @@ __device__ __forceinline__ void load_tile(const float2 *__restrict__ src, int nc
                                           float *im) {
     using C = XCfg<N>;
     constexpr int T = C::T;
-    for (int it = threadIdx.x; it < N * T; it += XT) {
-        const int t = it % T, x = it / T;
-        const int64_t l = l0 + t;
-        float2 v = make_float2(0.f, 0.f);
-        if (l < g.n2h) v = __ldg(src + (((int64_t)x * ncomp + comp) * g.n1 + j) * g.n2h + l);
-        const int q = Col<N, C::R2>::at(t, x);
-        re[q] = v.x;
-        im[q] = v.y;
+    constexpr int PER = N * T / XT;          // elements per thread
+    constexpr int CH = PER < 16 ? PER : 16;  // loads kept in flight per batch
+    const int t = threadIdx.x % T;           // this thread's column
+    const int x0 = threadIdx.x / T;          // and its first x (stride XT/T)
+    const int64_t l = l0 + t;
+    const bool ok = l < g.n2h;
+    const float2 *base = src + ((int64_t)comp * g.n1 + j) * g.n2h + l;
+    const int64_t xs = (int64_t)ncomp * g.n1 * g.n2h;
+#pragma unroll
+    for (int b = 0; b < PER; b += CH) {
+        float2 v[CH];
+#pragma unroll
+        for (int r = 0; r < CH; ++r) {
+            const int x = x0 + (b + r) * (XT / T);
+            v[r] = ok ? __ldg(base + x * xs) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int r = 0; r < CH; ++r) {
+            const int q = Col<N, C::R2>::at(t, x0 + (b + r) * (XT / T));
+            re[q] = v[r].x;
+            im[q] = v[r].y;
+        }
     }
 }
 
@@ -362,20 +376,31 @@ __global__ void __launch_bounds__(XT) k_xpass_adj(const float2 *__restrict__ Cin
         __syncthreads();
         // A = C_0;  B = i ky C_1 + i kz C_2   (i k (a + i b) = (-k b, k a))
         load_tile<N>(Cin, 3, 0, j, l0, g, are, aim);
-        for (int it = threadIdx.x; it < N * T; it += XT) {
-            const int t = it % T, x = it / T;
+        {
+            constexpr int PER = N * T / XT;
+            constexpr int CH = PER < 8 ? PER : 8;
+            const int t = threadIdx.x % T, x0 = threadIdx.x / T;
             const int64_t l = l0 + t;
-            float br = 0.f, bi = 0.f;
-            if (l < g.n2h) {
-                const float mzl = __ldg(mz + l);
-                const float2 *s = Cin + ((int64_t)x * 3 * g.n1 + j) * g.n2h + l;
-                const float2 c1 = __ldg(s + g.n1 * g.n2h), c2 = __ldg(s + 2 * g.n1 * g.n2h);
-                br = -__fadd_rn(__fmul_rn(myj, c1.y), __fmul_rn(mzl, c2.y));
-                bi = __fadd_rn(__fmul_rn(myj, c1.x), __fmul_rn(mzl, c2.x));
+            const bool ok = l < g.n2h;
+            const float mzl = ok ? __ldg(mz + l) : 0.f;
+            const int64_t cs = g.n1 * g.n2h, xs = 3 * cs;
+            const float2 *base = Cin + j * g.n2h + l;
+#pragma unroll
+            for (int b = 0; b < PER; b += CH) {
+                float2 c1[CH], c2[CH];
+#pragma unroll
+                for (int r = 0; r < CH; ++r) {
+                    const int x = x0 + (b + r) * (XT / T);
+                    c1[r] = ok ? __ldg(base + x * xs + cs) : make_float2(0.f, 0.f);
+                    c2[r] = ok ? __ldg(base + x * xs + 2 * cs) : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int r = 0; r < CH; ++r) {
+                    const int q = Col<N, R2>::at(t, x0 + (b + r) * (XT / T));
+                    bre[q] = -__fadd_rn(__fmul_rn(myj, c1[r].y), __fmul_rn(mzl, c2[r].y));
+                    bim[q] = __fadd_rn(__fmul_rn(myj, c1[r].x), __fmul_rn(mzl, c2[r].x));
+                }
             }
-            const int q = Col<N, R2>::at(t, x);
-            bre[q] = br;
-            bim[q] = bi;
         }
         __syncthreads();
         fft_fwd<N>(are, aim, tw);

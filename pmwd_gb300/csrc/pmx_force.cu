@@ -77,6 +77,7 @@ struct pmx_workspace {
     // power-of-two meshes: slab-wise 2-D cuFFT over (y, z) plus the fused
     // x pass of pmx_fft.cu; meshes are then plane-interleaved (x, 3, n1, n2)
     bool xfast = false;
+    bool win = false;           // warp-window deposits (n2 % 4 == 0)
     int64_t slab = 0;           // x-planes per 2-D cuFFT execution
     float2 *tw = nullptr;       // exp(-2 pi i m / n0)
     cufftHandle p2r = 0, p2c3 = 0, p2r3 = 0, p2c = 0;  // 2-D r2c, c2r x3, r2c x3, c2r
@@ -268,6 +269,8 @@ struct Hot {
     int64_t gxs, gjs;
     // optional Kahan compensation terms of disp and vel (n, 3); NULL = plain
     float *dcomp, *vcomp;
+    // deposit through per-warp shared-memory windows (needs n2 % 4 == 0)
+    bool win;
 };
 
 __device__ __forceinline__ void hot_axis(const Hot &h, int a, int pm, float d, Axis &ax) {
@@ -281,6 +284,7 @@ __device__ __forceinline__ void hot_axis(const Hot &h, int a, int pm, float d, A
         ax.s[nb] = sgnf(-d2);
         ax.i[nb] = pymod(ii + pm, h.wrap[a]);
     }
+    ax.u = fl + pm;
 }
 
 __device__ __forceinline__ int64_t hot_cell(const Hot &h, const Axis ax[3], int k) {
@@ -335,24 +339,128 @@ __device__ __forceinline__ void hot_deposit(const Hot &h, const Axis ax[3], floa
         atomicAdd(dens + hot_cell(h, ax, k), __fmul_rn(h.val, frac_of(ax, k)));
 }
 
+// ---------------------------------------------------------------------------
+// Warp deposit windows.  Particles are in Lagrangian (pmid-raveled) order, so
+// the 32 particles of a warp sit along one z row and their 8 neighbour cells
+// span 3 x 3 (x, y) rows of a short z range.  Each warp accumulates into a
+// shared-memory window of WROWS rows x WZ cells (z origin aligned to 4) with
+// shared atomics, then flushes it with one 16-byte red.global.add.v4.f32 per
+// four cells instead of one global atomic per contribution.  Contributions
+// outside the window go straight to global memory, so any particle order is
+// correct; the window only changes speed.  Needs n2 % 4 == 0 (16-byte groups).
+// ---------------------------------------------------------------------------
+
+constexpr int WZ = 80;      // window width along z (multiple of 4)
+constexpr int WROWS = 9;    // 3 x 3 (x, y) rows
+constexpr size_t WIN1_SMEM = (PT / 32) * WROWS * WZ * sizeof(float);  // one component
+constexpr size_t WIN3_SMEM = 3 * WIN1_SMEM;                           // three components
+
+struct Win {
+    int x0, y0, z0;         // unwrapped origin (z0 multiple of 4)
+};
+
+__device__ __forceinline__ int warp_min(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Origin of the warp's window from the lower-neighbour unwrapped indices of
+// its active lanes.
+__device__ __forceinline__ Win win_origin(bool act, const Axis ax[3]) {
+    Win w;
+    w.x0 = warp_min(act ? ax[0].u : INT_MAX);
+    w.y0 = warp_min(act ? ax[1].u : INT_MAX);
+    const int zm = warp_min(act ? ax[2].u : INT_MAX);
+    w.z0 = zm & ~3;  // floor to a multiple of 4 (two's complement)
+    return w;
+}
+
+// Adds v to neighbour k of this particle: into the warp window `buf`
+// (component stride WROWS*WZ) when inside it, else to global memory at
+// `gaddr`.
+__device__ __forceinline__ void win_add(float *buf, const Win &w, const Axis ax[3], int k, float v,
+                                        float *gaddr) {
+    const int dx = ax[0].u + (k & 1) - w.x0;
+    const int dy = ax[1].u + ((k >> 1) & 1) - w.y0;
+    const int dz = ax[2].u + ((k >> 2) & 1) - w.z0;
+    if ((unsigned)dx < 3u && (unsigned)dy < 3u && (unsigned)dz < (unsigned)WZ)
+        atomicAdd(buf + (dx * 3 + dy) * WZ + dz, v);
+    else
+        atomicAdd(gaddr, v);
+}
+
+// Flushes NC component windows of one warp to global memory with vector
+// reductions and zeroes them.  Global address of component c, cell
+// (x, y, z): c * cstride + x * xstride + y * n2 + z (wrapped), which covers
+// the density (NC = 1) and both mesh layouts of the cotangent meshes.
+template <int NC>
+__device__ __forceinline__ void win_flush(float *buf, const Win &w, const Hot &h, float *base,
+                                          int64_t xstride, int64_t cstride) {
+    const int lane = threadIdx.x & 31;
+    constexpr int G = WZ / 4;
+    for (int idx = lane; idx < NC * WROWS * G; idx += 32) {
+        const int c = idx / (WROWS * G);
+        const int r = (idx / G) % WROWS;
+        const int g = idx % G;
+        float4 *p = reinterpret_cast<float4 *>(buf + (c * WROWS + r) * WZ) + g;
+        const float4 v = *p;
+        if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
+            const int x = pymod(w.x0 + r / 3, h.wrap[0]);
+            const int y = pymod(w.y0 + r % 3, h.wrap[1]);
+            const int z = pymod(w.z0 + 4 * g, h.wrap[2]);
+            float *a = base + c * cstride + (int64_t)x * xstride + (int64_t)y * h.stride[1] + z;
+            atomicAdd(reinterpret_cast<float4 *>(a), v);
+            *p = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+}
+
+__device__ __forceinline__ void win_zero(float *buf, int nfloats) {
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < nfloats; i += 32) buf[i] = 0.f;
+}
+
 // Forward: optional kick (vel += acc*K1) and drift (disp += vel*D), then the
 // CIC density deposit of the (new) positions.
 template <bool KD>
 __global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ pmid, float *disp,
                                             float *vel, const float *__restrict__ acc, int64_t n,
                                             float K1, float D, float *dens) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        float3 d = ld3(disp, q);
-        if (KD) {
-            float3 v = kahan_axpy(ld3(vel, q), ld3(acc, q), K1, h.vcomp, q);
-            d = kahan_axpy(d, v, D, h.dcomp, q);
-            st3(vel, q, v);
-            st3(disp, q, d);
-        }
+    extern __shared__ __align__(16) float wsm[];
+    const int lane = threadIdx.x & 31;
+    float *buf = wsm + (threadIdx.x >> 5) * (WROWS * WZ);
+    if (h.win) win_zero(buf, WROWS * WZ);
+    __syncwarp();
+    // warp-uniform loop: each warp takes 32 consecutive particles
+    for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); q0 < n;
+         q0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = q0 + lane;
+        const bool act = q < n;
         Axis ax[3];
-        hot_enmesh(h, pmid, q, d, ax);
-        hot_deposit(h, ax, dens);
+        if (act) {
+            float3 d = ld3(disp, q);
+            if (KD) {
+                float3 v = kahan_axpy(ld3(vel, q), ld3(acc, q), K1, h.vcomp, q);
+                d = kahan_axpy(d, v, D, h.dcomp, q);
+                st3(vel, q, v);
+                st3(disp, q, d);
+            }
+            hot_enmesh(h, pmid, q, d, ax);
+        }
+        if (!h.win) {
+            if (act) hot_deposit(h, ax, dens);
+            continue;
+        }
+        const Win w = win_origin(act, ax);
+        if (act) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                win_add(buf, w, ax, k, __fmul_rn(h.val, frac_of(ax, k)), dens + hot_cell(h, ax, k));
+        }
+        __syncwarp();
+        win_flush<1>(buf, w, h, dens, h.stride[0], 0);
+        __syncwarp();
     }
 }
 
@@ -392,27 +500,48 @@ __global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pm
                                            const float *__restrict__ alpha, int64_t n, float K1,
                                            float D, float *dens, double *part) {
     __shared__ double sh[PT / 32];
+    extern __shared__ __align__(16) float wsm[];
+    const int lane = threadIdx.x & 31;
+    float *buf = wsm + (threadIdx.x >> 5) * (WROWS * WZ);
+    if (h.win) win_zero(buf, WROWS * WZ);
+    __syncwarp();
     double s0 = 0.0, s1 = 0.0;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        float3 d = ld3(disp, q);
-        if (KD) {
-            float3 a = ld3(acc, q);
-            float3 vc = ld3(vel_cot, q);
-            float3 v = kahan_axpy(ld3(vel, q), a, K1, h.vcomp, q);
-            float3 dc = axmy3(ld3(disp_cot, q), ld3(alpha, q), K1);
-            s0 += dot3d(vc, a);
-            d = kahan_axpy(d, v, D, h.dcomp, q);
-            vc = axmy3(vc, dc, D);
-            s1 += dot3d(dc, v);
-            st3(vel, q, v);
-            st3(disp, q, d);
-            st3(disp_cot, q, dc);
-            st3(vel_cot, q, vc);
-        }
+    for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); q0 < n;
+         q0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = q0 + lane;
+        const bool act = q < n;
         Axis ax[3];
-        hot_enmesh(h, pmid, q, d, ax);
-        hot_deposit(h, ax, dens);
+        if (act) {
+            float3 d = ld3(disp, q);
+            if (KD) {
+                float3 a = ld3(acc, q);
+                float3 vc = ld3(vel_cot, q);
+                float3 v = kahan_axpy(ld3(vel, q), a, K1, h.vcomp, q);
+                float3 dc = axmy3(ld3(disp_cot, q), ld3(alpha, q), K1);
+                s0 += dot3d(vc, a);
+                d = kahan_axpy(d, v, D, h.dcomp, q);
+                vc = axmy3(vc, dc, D);
+                s1 += dot3d(dc, v);
+                st3(vel, q, v);
+                st3(disp, q, d);
+                st3(disp_cot, q, dc);
+                st3(vel_cot, q, vc);
+            }
+            hot_enmesh(h, pmid, q, d, ax);
+        }
+        if (!h.win) {
+            if (act) hot_deposit(h, ax, dens);
+            continue;
+        }
+        const Win w = win_origin(act, ax);
+        if (act) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                win_add(buf, w, ax, k, __fmul_rn(h.val, frac_of(ax, k)), dens + hot_cell(h, ax, k));
+        }
+        __syncwarp();
+        win_flush<1>(buf, w, h, dens, h.stride[0], 0);
+        __syncwarp();
     }
     if (KD) {
         double t0 = block_sum<PT>(s0, sh);
@@ -435,39 +564,67 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
                                               const float *__restrict__ g, float *mcot,
                                               double *part) {
     __shared__ double sh[PT / 32];
+    extern __shared__ __align__(16) float wsm[];
+    const int lane = threadIdx.x & 31;
+    float *buf = wsm + (threadIdx.x >> 5) * (3 * WROWS * WZ);
+    if (h.win) win_zero(buf, 3 * WROWS * WZ);
+    __syncwarp();
     double s2 = 0.0;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
-         q += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); q0 < n;
+         q0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = q0 + lane;
+        const bool act = q < n;
         Axis ax[3];
-        hot_enmesh(h, pmid, q, ld3(disp, q), ax);
-        float3 vc = ld3(vel_cot, q);
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-        float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+        float3 vc = make_float3(0.f, 0.f, 0.f);
+        if (act) {
+            hot_enmesh(h, pmid, q, ld3(disp, q), ax);
+            vc = ld3(vel_cot, q);
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+            float c0 = 0.f, c1 = 0.f, c2 = 0.f;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            int64_t c = hot_cell(h, ax, k);
-            float f = frac_of(ax, k);
-            float fg[3];
-            frac_grad_of(ax, k, fg);
-            const int64_t gc = c + (int64_t)ax[0].i[k & 1] * h.gxs;
-            float m0 = __ldg(g + gc), m1 = __ldg(g + gc + h.gjs), m2 = __ldg(g + gc + 2 * h.gjs);
-            a0 = __fadd_rn(a0, __fmul_rn(m0, f));
-            a1 = __fadd_rn(a1, __fmul_rn(m1, f));
-            a2 = __fadd_rn(a2, __fmul_rn(m2, f));
-            float t = __fadd_rn(__fadd_rn(__fmul_rn(vc.x, m0), __fmul_rn(vc.y, m1)),
-                                __fmul_rn(vc.z, m2));
-            c0 = __fadd_rn(c0, __fmul_rn(t, fg[0]));
-            c1 = __fadd_rn(c1, __fmul_rn(t, fg[1]));
-            c2 = __fadd_rn(c2, __fmul_rn(t, fg[2]));
-            atomicAdd(mcot + gc, __fmul_rn(vc.x, f));
-            atomicAdd(mcot + gc + h.gjs, __fmul_rn(vc.y, f));
-            atomicAdd(mcot + gc + 2 * h.gjs, __fmul_rn(vc.z, f));
+            for (int k = 0; k < 8; ++k) {
+                int64_t c = hot_cell(h, ax, k);
+                float f = frac_of(ax, k);
+                float fg[3];
+                frac_grad_of(ax, k, fg);
+                const int64_t gc = c + (int64_t)ax[0].i[k & 1] * h.gxs;
+                float m0 = __ldg(g + gc), m1 = __ldg(g + gc + h.gjs), m2 = __ldg(g + gc + 2 * h.gjs);
+                a0 = __fadd_rn(a0, __fmul_rn(m0, f));
+                a1 = __fadd_rn(a1, __fmul_rn(m1, f));
+                a2 = __fadd_rn(a2, __fmul_rn(m2, f));
+                float t = __fadd_rn(__fadd_rn(__fmul_rn(vc.x, m0), __fmul_rn(vc.y, m1)),
+                                    __fmul_rn(vc.z, m2));
+                c0 = __fadd_rn(c0, __fmul_rn(t, fg[0]));
+                c1 = __fadd_rn(c1, __fmul_rn(t, fg[1]));
+                c2 = __fadd_rn(c2, __fmul_rn(t, fg[2]));
+                if (!h.win) {
+                    atomicAdd(mcot + gc, __fmul_rn(vc.x, f));
+                    atomicAdd(mcot + gc + h.gjs, __fmul_rn(vc.y, f));
+                    atomicAdd(mcot + gc + 2 * h.gjs, __fmul_rn(vc.z, f));
+                }
+            }
+            float3 a = make_float3(a0, a1, a2);
+            st3(acc, q, a);
+            st3(alpha, q, make_float3(__fdiv_rn(c0, h.cell), __fdiv_rn(c1, h.cell),
+                                      __fdiv_rn(c2, h.cell)));
+            s2 += dot3d(vc, a);
         }
-        float3 a = make_float3(a0, a1, a2);
-        st3(acc, q, a);
-        st3(alpha, q, make_float3(__fdiv_rn(c0, h.cell), __fdiv_rn(c1, h.cell),
-                                  __fdiv_rn(c2, h.cell)));
-        s2 += dot3d(vc, a);
+        if (!h.win) continue;
+        // gather-VJP mesh term through the warp window, three components
+        const Win w = win_origin(act, ax);
+        if (act) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const float f = frac_of(ax, k);
+                const int64_t gc = hot_cell(h, ax, k) + (int64_t)ax[0].i[k & 1] * h.gxs;
+                win_add(buf, w, ax, k, __fmul_rn(vc.x, f), mcot + gc);
+                win_add(buf + WROWS * WZ, w, ax, k, __fmul_rn(vc.y, f), mcot + gc + h.gjs);
+                win_add(buf + 2 * WROWS * WZ, w, ax, k, __fmul_rn(vc.z, f), mcot + gc + 2 * h.gjs);
+            }
+        }
+        __syncwarp();
+        win_flush<3>(buf, w, h, mcot, h.stride[0] + h.gxs, h.gjs);
+        __syncwarp();
     }
     double t2 = block_sum<PT>(s2, sh);
     if (threadIdx.x == 0) part[2 * PMAX + blockIdx.x] = t2;
@@ -646,6 +803,7 @@ int check_hot(pmx_workspace *ws, const pmx_enmesh_spec *spec, const void *pmid, 
     h->val = (float)((double)ws->M / (double)ptcl_num);
     h->dcomp = nullptr;
     h->vcomp = nullptr;
+    h->win = ws->win;
     if (ws->xfast) {
         h->gxs = 2 * ws->n1 * ws->n2;
         h->gjs = ws->n1 * ws->n2;
@@ -913,6 +1071,16 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
         ws_free(ws);
         return st;
     }
+    const char *wenv = std::getenv("PMX_WIN");
+    ws->win = (ws->n2 % 4 == 0) && !(flags & PMX_WS_NO_WINDOW) && !(wenv && wenv[0] == '0');
+    if (ws->win) {
+        cudaError_t e = cudaFuncSetAttribute(k_g3adj, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)WIN3_SMEM);
+        if (e != cudaSuccess) {
+            ws_free(ws);
+            return cuda_status(e, "cudaFuncSetAttribute(k_g3adj)");
+        }
+    }
     const char *xenv = std::getenv("PMX_XFAST");
     ws->xfast = xpass_supported(ws->n0) && !(flags & PMX_WS_CUFFT3D) && !(xenv && xenv[0] == '0');
     size_t wk[4] = {0, 0, 0, 0};
@@ -997,7 +1165,7 @@ extern "C" int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec, const i
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
-            k_kds<false><<<stride_grid(n, PT), PT, 0, s>>>(h, pmid, const_cast<float *>(disp), nullptr,
+            k_kds<false><<<stride_grid(n, PT), PT, WIN1_SMEM, s>>>(h, pmid, const_cast<float *>(disp), nullptr,
                                                           nullptr, n, 0.f, 0.f, ws->dens);
             PMX_LAUNCH_CHECK("k_kds");
         }
@@ -1036,7 +1204,7 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
-            k_kds<false><<<G, PT, 0, s>>>(h, pmid, const_cast<float *>(disp), nullptr, nullptr, n, 0.f,
+            k_kds<false><<<G, PT, WIN1_SMEM, s>>>(h, pmid, const_cast<float *>(disp), nullptr, nullptr, n, 0.f,
                                           0.f, ws->dens);
             PMX_LAUNCH_CHECK("k_kds");
         }
@@ -1045,7 +1213,7 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
     if (n > 0) {
         {
             Stage sg(ws, 7, s, 1);
-            k_g3adj<<<G, PT, 0, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M, ws->g, ws->mcot,
+            k_g3adj<<<G, PT, WIN3_SMEM, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M, ws->g, ws->mcot,
                                      ws->part);
             PMX_LAUNCH_CHECK("k_g3adj");
         }
@@ -1184,7 +1352,7 @@ static int nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int1
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
-            k_kds<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, factors[0], factors[1], ws->dens);
+            k_kds<true><<<G, PT, WIN1_SMEM, s>>>(h, pmid, disp, vel, acc, n, factors[0], factors[1], ws->dens);
             PMX_LAUNCH_CHECK("k_kds");
         }
     }
@@ -1229,14 +1397,14 @@ static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const 
     if (G > PMAX) G = PMAX;
     {
         Stage sg(ws, 6, s, 1);
-        k_ka<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n, factors[0],
+        k_ka<true><<<G, PT, WIN1_SMEM, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n, factors[0],
                                     factors[1], ws->dens, ws->part);
         PMX_LAUNCH_CHECK("k_ka");
     }
     if ((st = force_meshes(ws, h, omega_m, s))) return st;
     {
         Stage sg(ws, 7, s, 1);
-        k_g3adj<<<G, PT, 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M, ws->g, ws->mcot,
+        k_g3adj<<<G, PT, WIN3_SMEM, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M, ws->g, ws->mcot,
                                  ws->part);
         PMX_LAUNCH_CHECK("k_g3adj");
     }

@@ -112,6 +112,7 @@ struct Axis {
     int i[2];
     float w[2];
     float s[2];
+    int u;  // unwrapped index of the lower neighbour (hot path only)
 };
 
 __device__ __forceinline__ void enmesh_axis(const EmParams &p, int a, int pm, float d,

@@ -178,8 +178,10 @@ def test_fused_step_equals_generic_ops(cuda, nb_case):
     assert not gnb._is_fused(gconf2)
     generic = _run_gpu_nbody(gconf2, pmid, disp, vel, pg.boltzmann(pg.SimpleLCDM(gconf2), gconf2),
                              cuda)
-    assert rel_l2(generic.disp.cpu().numpy(), fused.disp.cpu().numpy()) < 1e-6
-    assert rel_l2(generic.vel.cpu().numpy(), fused.vel.cpu().numpy()) < 1e-6
+    # only the order of the float32 atomic adds differs (8 steps amplify it
+    # to ~1e-6)
+    assert rel_l2(generic.disp.cpu().numpy(), fused.disp.cpu().numpy()) < 1e-5
+    assert rel_l2(generic.vel.cpu().numpy(), fused.vel.cpu().numpy()) < 1e-5
 
 
 def test_factors_match_oracle(nb_case):
@@ -261,3 +263,34 @@ def test_reversibility_plain_and_kahan(cuda):
     for ed, ev in errs.values():
         assert ed < 2e-3 and ev < 2e-3
     assert errs[True][0] <= 1.5 * errs[False][0] + 1e-7
+
+
+@pytest.mark.parametrize('shuffle', [False, True], ids=['lagrangian', 'shuffled'])
+def test_window_deposit_equals_direct_atomics(cuda, shuffle):
+    """Warp-window deposits (shared-memory accumulation flushed with 16-byte
+    vector reductions) give the same force and VJP as one global atomic per
+    contribution; a shuffled particle order sends most contributions through
+    the window's fallback path."""
+    oconf, gconf, pmid, disp, vel = make((32, 32, 32), 2, 1.0, 2.0)
+    if shuffle:
+        perm = np.random.default_rng(5).permutation(len(pmid))
+        pmid, disp = pmid[perm], disp[perm]
+    cot = np.random.default_rng(6).normal(size=disp.shape).astype(np.float32)
+    acc_o = pm.gravity(pmid, disp, 0.3, oconf)
+    out = []
+    for window in (True, False):
+        ws = _lib.Workspace(gconf.mesh_shape, adjoint=True, window=window)
+        spec = _lib.make_spec(3, gconf.mesh_shape, gconf.mesh_shape, gconf.cell_size)
+        n = len(pmid)
+        acc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+        dc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+        om = torch.zeros((), dtype=torch.float64, device=cuda)
+        _lib.call('pmx_force_vjp', ws.handle, spec, T(pmid, cuda), T(disp, cuda), n,
+                  gconf.ptcl_num, 0.3, T(cot, cuda), acc, dc, om, _lib.stream_ptr(cuda))
+        out.append((acc.cpu().numpy(), dc.cpu().numpy(), float(om)))
+        del ws
+    (a1, d1, o1), (a2, d2, o2) = out
+    assert rel_l2(a1, acc_o) < RTOL_ACC
+    assert rel_l2(a1, a2) < 1e-6
+    assert rel_l2(d1, d2) < 1e-5
+    assert abs(o1 / o2 - 1) < 1e-6
