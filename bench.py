@@ -52,6 +52,10 @@ def parse():
                     help='particle grid side of the bounded CPU sample')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--serve', type=int, default=0,
+                    help='serving mode: number of requests of the serving stream')
+    ap.add_argument('--serve-sides', default='64,128,256')
+    ap.add_argument('--serve-steps', default='10,100')
     return ap.parse_args()
 
 
@@ -430,6 +434,35 @@ def run_pmx(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """Serving stream (mixed grids, mesh factors, step counts, cosmologies,
+    20% gradients) served with continuous batching vs one at a time, same
+    requests; then the served form under Poisson arrivals at 80% of its
+    throughput for p50/p99 latency."""
+    import torch
+    from pmwd_gb300 import serving
+    torch.cuda.set_device(0)
+    sides = tuple(int(s) for s in args.serve_sides.split(','))
+    steps = tuple(int(s) for s in args.serve_steps.split(','))
+    reqs = serving.make_stream(args.serve, rate_hz=0.0, seed=0, sides=sides, steps=steps)
+    warm = serving.make_stream(4, rate_hz=0.0, seed=1, sides=sides[:1], steps=(2, 3))
+    serving.run_sequential(warm)
+    _, seq = serving.run_sequential(reqs)
+    _, srv = serving.Server(budget_bytes=150e9).run(reqs, realtime=False)
+    rate = 0.8 * srv['sims_per_s']
+    timed = serving.make_stream(args.serve, rate_hz=rate, seed=0, sides=sides, steps=steps)
+    _, rt = serving.Server(budget_bytes=150e9).run(timed, realtime=True)
+    line = {'metric': 'served sims/s', 'value': srv['sims_per_s'], 'unit': 'sims/s',
+            'higher_is_better': True, 'n_gpus': 1,
+            'sequential_sims_per_s': seq['sims_per_s'],
+            'speedup_vs_sequential': srv['sims_per_s'] / seq['sims_per_s'],
+            'poisson_rate_hz': rate, 'p50_s': rt['p50_s'], 'p99_s': rt['p99_s'],
+            'realtime_sims_per_s': rt['sims_per_s'],
+            'config': {'workload': f'{args.serve} requests, ptcl grid {sides}^3, mesh factor '
+                                   f'{{1,2}}, steps U{steps}, 20% gradients, HBM budget 150 GB'}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get('RANK', 0))
@@ -437,6 +470,10 @@ def main():
     local_rank = int(os.environ.get('LOCAL_RANK', 0))
     if args.impl == 'reference':
         run_reference(args, rank)
+        return
+    if args.serve:
+        if rank == 0:
+            run_serve(args)
         return
     if world > 1:
         import torch
