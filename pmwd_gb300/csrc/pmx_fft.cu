@@ -18,12 +18,13 @@
 // c = 1.5 Omega_m / N folds in the real-space scale and irfftn's 1/N.
 //
 // One CTA transforms T columns (fixed ky, T consecutive kz) of length n0
-// held in shared memory as split re/im float arrays.  The length-n0 FFT is
-// a six-step transform n0 = R1 * R2: R2-strided DFTs of length R1 with
-// twiddles, then contiguous DFTs of length R2; each DFT runs in registers
-// (radix-2, unrolled).  The forward leaves the spectrum in the transposed
-// order p = k1*R2 + k2 <-> kx = k1 + R1*k2, which the inverse consumes
-// directly and returns to natural order, so no reordering pass is needed.
+// held in shared memory as padded complex (float2) buffers.  The length-n0
+// FFT is a six-step transform n0 = R1 * R2: R2-strided DFTs of length R1
+// with twiddles, then contiguous DFTs of length R2; each DFT runs in
+// registers (radix-2, unrolled).  The second step, the Fourier-space
+// operator and the first inverse step all act on the same contiguous group
+// of R2 values, so one thread does them back to back in registers; the
+// spectrum never needs natural order and no reordering pass exists.
 
 #include <cuda_runtime.h>
 
@@ -121,14 +122,44 @@ __device__ __forceinline__ void dft(float (&re)[R], float (&im)[R]) {
 // bit reversal of the low `bits` bits
 __device__ __forceinline__ int brev(int k, int bits) { return (int)(__brev((unsigned)k) >> (32 - bits)); }
 
-// Column buffer geometry: column t of length N stored at t*CS, logical
-// position p at p + p/R2 (one pad float per R2 values, so both the strided
-// and the contiguous DFT steps are free of bank conflicts).
-template <int N, int R2>
-struct Col {
-    static constexpr int CS = N + N / R2;
-    __device__ static __forceinline__ int at(int t, int p) { return t * CS + p + p / R2; }
-};
+
+constexpr int cbrev(int k, int bits) {
+    int r = 0;
+    for (int b = 0; b < bits; ++b) r |= ((k >> b) & 1) << (bits - 1 - b);
+    return r;
+}
+
+// out[i] = in[brev(i)]: bit-reversed register order -> natural order, with
+// compile-time indices (fold expression).
+template <int R, int... Is>
+__device__ __forceinline__ void unbrev_impl(const float2 (&in)[R], float2 (&out)[R],
+                                            std::integer_sequence<int, Is...>) {
+    ((out[Is] = in[cbrev(Is, Log2<R>::v)]), ...);
+}
+template <int R>
+__device__ __forceinline__ void unbrev(const float2 (&in)[R], float2 (&out)[R]) {
+    unbrev_impl<R>(in, out, std::make_integer_sequence<int, R>{});
+}
+
+// float2 wrappers of the split-array register DFT
+template <int R, bool INV, int... Is>
+__device__ __forceinline__ void dft2_impl(float2 (&v)[R], std::integer_sequence<int, Is...>) {
+    float re[R], im[R];
+    ((re[Is] = v[Is].x, im[Is] = v[Is].y), ...);
+    dft<R, INV>(re, im);
+    ((v[Is] = make_float2(re[Is], im[Is])), ...);
+}
+template <int R, bool INV>
+__device__ __forceinline__ void dft2(float2 (&v)[R]) {
+    dft2_impl<R, INV>(v, std::make_integer_sequence<int, R>{});
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a * conj(b)
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
 
 template <int N>
 struct Split;  // N = R1 * R2
@@ -140,109 +171,72 @@ template <> struct Split<1024> { static constexpr int R1 = 32, R2 = 32; };
 
 constexpr int XT = 256;  // threads per x-pass CTA
 
+// Column buffers of complex (float2) values: column t at t*CS, logical
+// position p at p + p/R2 (one pad per R2 values keeps the strided and the
+// contiguous DFT steps free of bank conflicts for 8-byte accesses; the +1
+// per column does the same for the tile loads and stores).
 template <int N>
 struct XCfg {
     static constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2;
     static constexpr int RM = R1 > R2 ? R1 : R2;
     static constexpr int T = XT / RM;  // columns per CTA
-    static constexpr int CS = Col<N, R2>::CS;
-    static constexpr int BUF = T * CS;  // floats per re (or im) buffer
+    static constexpr int CS = N + N / R2 + 1;
+    static constexpr int BUF = T * CS;  // float2 per buffer
+    __device__ static __forceinline__ int at(int t, int p) { return t * CS + p + p / R2; }
 };
 
-// Forward FFT (natural -> transposed order) of the T columns in (re, im).
-// tw = exp(-2 pi i m / N), m in [0, N).
+// Forward step 1 on one buffer: R2-strided radix-R1 DFTs + twiddles,
+// natural order -> "transposed" positions k1*R2 + b.
 template <int N>
-__device__ __forceinline__ void fft_fwd(float *re, float *im, const float2 *tw) {
+__device__ __forceinline__ void fwd_step1(float2 *buf, const float2 *tw) {
     using C = XCfg<N>;
     constexpr int R1 = C::R1, R2 = C::R2;
     for (int it = threadIdx.x; it < C::T * R2; it += XT) {
         const int t = it / R2, b = it % R2;
-        float xr[R1], xi[R1];
+        float2 v[R1];
 #pragma unroll
-        for (int a = 0; a < R1; ++a) {
-            const int q = Col<N, R2>::at(t, a * R2 + b);
-            xr[a] = re[q];
-            xi[a] = im[q];
-        }
-        dft<R1, false>(xr, xi);
+        for (int a = 0; a < R1; ++a) v[a] = buf[C::at(t, a * R2 + b)];
+        dft2<R1, false>(v);
 #pragma unroll
         for (int k = 0; k < R1; ++k) {
             const int k1 = brev(k, Log2<R1>::v);
-            const float2 w = tw[(b * k1) & (N - 1)];
-            const float r = xr[k] * w.x - xi[k] * w.y;
-            const float i = xr[k] * w.y + xi[k] * w.x;
-            const int q = Col<N, R2>::at(t, k1 * R2 + b);
-            re[q] = r;
-            im[q] = i;
+            buf[C::at(t, k1 * R2 + b)] = cmul(v[k], tw[b * k1]);
         }
     }
-    __syncthreads();
-    for (int it = threadIdx.x; it < C::T * R1; it += XT) {
-        const int t = it / R1, k1 = it % R1;
-        float xr[R2], xi[R2];
-#pragma unroll
-        for (int b = 0; b < R2; ++b) {
-            const int q = Col<N, R2>::at(t, k1 * R2 + b);
-            xr[b] = re[q];
-            xi[b] = im[q];
-        }
-        dft<R2, false>(xr, xi);
-#pragma unroll
-        for (int k = 0; k < R2; ++k) {
-            const int q = Col<N, R2>::at(t, k1 * R2 + brev(k, Log2<R2>::v));
-            re[q] = xr[k];
-            im[q] = xi[k];
-        }
-    }
-    __syncthreads();
 }
 
-// Unnormalised inverse FFT (transposed -> natural order), the exact
-// reversal of fft_fwd's index maps.
+// Inverse step 1 (the last inverse step) on one buffer: radix-R1 inverse
+// DFTs over k1 at fixed b -> natural order.
 template <int N>
-__device__ __forceinline__ void fft_inv(float *re, float *im, const float2 *tw) {
+__device__ __forceinline__ void inv_step1(float2 *buf) {
     using C = XCfg<N>;
     constexpr int R1 = C::R1, R2 = C::R2;
-    for (int it = threadIdx.x; it < C::T * R1; it += XT) {
-        const int t = it / R1, k1 = it % R1;
-        float xr[R2], xi[R2];
-#pragma unroll
-        for (int k2 = 0; k2 < R2; ++k2) {
-            const int q = Col<N, R2>::at(t, k1 * R2 + k2);
-            xr[k2] = re[q];
-            xi[k2] = im[q];
-        }
-        dft<R2, true>(xr, xi);
-#pragma unroll
-        for (int k = 0; k < R2; ++k) {
-            const int b = brev(k, Log2<R2>::v);
-            const float2 w = tw[(b * k1) & (N - 1)];  // conj(w) below
-            const float r = xr[k] * w.x + xi[k] * w.y;
-            const float i = xi[k] * w.x - xr[k] * w.y;
-            const int q = Col<N, R2>::at(t, k1 * R2 + b);
-            re[q] = r;
-            im[q] = i;
-        }
-    }
-    __syncthreads();
     for (int it = threadIdx.x; it < C::T * R2; it += XT) {
         const int t = it / R2, b = it % R2;
-        float xr[R1], xi[R1];
+        float2 v[R1];
 #pragma unroll
-        for (int k1 = 0; k1 < R1; ++k1) {
-            const int q = Col<N, R2>::at(t, k1 * R2 + b);
-            xr[k1] = re[q];
-            xi[k1] = im[q];
-        }
-        dft<R1, true>(xr, xi);
+        for (int k1 = 0; k1 < R1; ++k1) v[k1] = buf[C::at(t, k1 * R2 + b)];
+        dft2<R1, true>(v);
 #pragma unroll
-        for (int k = 0; k < R1; ++k) {
-            const int q = Col<N, R2>::at(t, brev(k, Log2<R1>::v) * R2 + b);
-            re[q] = xr[k];
-            im[q] = xi[k];
-        }
+        for (int k = 0; k < R1; ++k) buf[C::at(t, brev(k, Log2<R1>::v) * R2 + b)] = v[k];
     }
-    __syncthreads();
+}
+
+// Inverse step 2 on a register group in bit-reversed k2 order (as the
+// forward step 2 leaves it), twiddle, store to positions k1*R2 + b.
+template <int N>
+__device__ __forceinline__ void inv_step2_store(float2 (&v)[XCfg<N>::R2], float2 *buf, int t,
+                                                int k1, const float2 *tw) {
+    using C = XCfg<N>;
+    constexpr int R2 = C::R2;
+    float2 u[R2];
+    unbrev<R2>(v, u);           // natural k2 order
+    dft2<R2, true>(u);          // element k holds b = brev(k)
+#pragma unroll
+    for (int k = 0; k < R2; ++k) {
+        const int b = brev(k, Log2<R2>::v);
+        buf[C::at(t, k1 * R2 + b)] = cmulc(u[k], tw[b * k1]);
+    }
 }
 
 struct XGeom {
@@ -251,18 +245,18 @@ struct XGeom {
     float c;              // 1.5 Omega_m / N
 };
 
-// Loads column tile (fixed ky row j, kz in [l0, l0+T)) of a complex array
-// laid out (x, comp, n1, n2h) with `ncomp` components; component `comp`.
+// Loads the column tile (fixed ky row j, kz in [l0, l0+T), all x) of a
+// complex array laid out (x, ncomp, n1, n2h), component `comp`; optionally
+// combines two components: out = (i k1m) in1 + (i k2m) in2.
 template <int N>
 __device__ __forceinline__ void load_tile(const float2 *__restrict__ src, int ncomp, int comp,
-                                          int64_t j, int64_t l0, const XGeom &g, float *re,
-                                          float *im) {
+                                          int64_t j, int64_t l0, const XGeom &g, float2 *buf) {
     using C = XCfg<N>;
     constexpr int T = C::T;
-    constexpr int PER = N * T / XT;          // elements per thread
-    constexpr int CH = PER < 16 ? PER : 16;  // loads kept in flight per batch
-    const int t = threadIdx.x % T;           // this thread's column
-    const int x0 = threadIdx.x / T;          // and its first x (stride XT/T)
+    constexpr int PER = N * T / XT;
+    constexpr int CH = PER < 16 ? PER : 16;
+    const int t = threadIdx.x % T;
+    const int x0 = threadIdx.x / T;
     const int64_t l = l0 + t;
     const bool ok = l < g.n2h;
     const float2 *base = src + ((int64_t)comp * g.n1 + j) * g.n2h + l;
@@ -276,11 +270,7 @@ __device__ __forceinline__ void load_tile(const float2 *__restrict__ src, int nc
             v[r] = ok ? __ldg(base + x * xs) : make_float2(0.f, 0.f);
         }
 #pragma unroll
-        for (int r = 0; r < CH; ++r) {
-            const int q = Col<N, C::R2>::at(t, x0 + (b + r) * (XT / T));
-            re[q] = v[r].x;
-            im[q] = v[r].y;
-        }
+        for (int r = 0; r < CH; ++r) buf[C::at(t, x0 + (b + r) * (XT / T))] = v[r];
     }
 }
 
@@ -292,10 +282,9 @@ __global__ void __launch_bounds__(XT) k_xpass_fwd(const float2 *__restrict__ H,
                                                   int64_t n0) {
     using C = XCfg<N>;
     constexpr int T = C::T, R1 = C::R1, R2 = C::R2;
-    extern __shared__ float smem[];
-    float *are = smem, *aim = smem + C::BUF;
-    float *bre = smem + 2 * C::BUF, *bim = smem + 3 * C::BUF;
-    float2 *tw = reinterpret_cast<float2 *>(smem + 4 * C::BUF);
+    extern __shared__ __align__(16) float2 smem2[];
+    float2 *A = smem2, *B = smem2 + C::BUF;
+    float2 *tw = smem2 + 2 * C::BUF;
     for (int m = threadIdx.x; m < N; m += XT) tw[m] = twg[m];
 
     const int64_t tot = n0 + g.n1 + g.n2h;
@@ -305,48 +294,57 @@ __global__ void __launch_bounds__(XT) k_xpass_fwd(const float2 *__restrict__ H,
     for (int64_t tile = blockIdx.x; tile < g.n1 * g.ncol_tiles; tile += gridDim.x) {
         const int64_t j = tile / g.ncol_tiles;
         const int64_t l0 = (tile % g.ncol_tiles) * T;
-        __syncthreads();  // previous tile's buffers are free
-        load_tile<N>(H, 1, 0, j, l0, g, are, aim);
+        __syncthreads();  // buffers free (also orders the twiddle fill)
+        load_tile<N>(H, 1, 0, j, l0, g, A);
         __syncthreads();
-        fft_fwd<N>(are, aim, tw);
-        // P = -(c/k^2) F in A;  B = -i kx P
+        fwd_step1<N>(A, tw);
+        __syncthreads();
+        // fused: forward step 2, Green + gradient, inverse step 2 of P and of
+        // B = -i kx P, all on one thread's contiguous group
         const float kyj = __ldg(ky + j), myj = __ldg(my + j);
         const float ky2 = __fmul_rn(kyj, kyj);
-        for (int it = threadIdx.x; it < N * T; it += XT) {
-            const int t = it / N, p = it % N;
-            const int k1 = p / R2, k2 = p % R2;
-            const int ix = k1 + R1 * k2;
+        for (int it = threadIdx.x; it < T * R1; it += XT) {
+            const int t = it / R1, k1 = it % R1;
             const int64_t l = l0 + t;
-            const float kxi = __ldg(kx + ix), mxi = __ldg(mx + ix);
             const float kzl = l < g.n2h ? __ldg(kz + l) : 0.f;
-            const float k2v = __fadd_rn(__fadd_rn(__fmul_rn(kxi, kxi), ky2), __fmul_rn(kzl, kzl));
-            const int q = Col<N, R2>::at(t, p);
-            float pr = 0.f, pi = 0.f;
-            if (k2v != 0.f) {
-                pr = -__fdiv_rn(__fmul_rn(are[q], g.c), k2v);
-                pi = -__fdiv_rn(__fmul_rn(aim[q], g.c), k2v);
+            const float kz2 = __fmul_rn(kzl, kzl);
+            float2 v[R2];
+#pragma unroll
+            for (int b = 0; b < R2; ++b) v[b] = A[C::at(t, k1 * R2 + b)];
+            dft2<R2, false>(v);          // element k: kx index k1 + R1*brev(k)
+            float2 w[R2];
+#pragma unroll
+            for (int k = 0; k < R2; ++k) {
+                const int ix = k1 + R1 * brev(k, Log2<R2>::v);
+                const float kxi = __ldg(kx + ix), mxi = __ldg(mx + ix);
+                const float k2v = __fadd_rn(__fadd_rn(__fmul_rn(kxi, kxi), ky2), kz2);
+                float pr = 0.f, pi = 0.f;
+                if (k2v != 0.f) {
+                    pr = -__fdiv_rn(__fmul_rn(v[k].x, g.c), k2v);
+                    pi = -__fdiv_rn(__fmul_rn(v[k].y, g.c), k2v);
+                }
+                v[k] = make_float2(pr, pi);
+                w[k] = make_float2(__fmul_rn(mxi, pi), -__fmul_rn(mxi, pr));  // -i kx P
             }
-            are[q] = pr;
-            aim[q] = pi;
-            // (-i k)(pr + i pi) = (k pi, -k pr)
-            bre[q] = __fmul_rn(mxi, pi);
-            bim[q] = -__fmul_rn(mxi, pr);
+            inv_step2_store<N>(v, A, t, k1, tw);
+            inv_step2_store<N>(w, B, t, k1, tw);
         }
         __syncthreads();
-        fft_inv<N>(bre, bim, tw);
-        fft_inv<N>(are, aim, tw);
-        // G_0 = B; G_1 = -i ky Q; G_2 = -i kz Q  (Q in A), layout (x, 3, n1, n2h)
+        inv_step1<N>(A);
+        inv_step1<N>(B);
+        __syncthreads();
+        // G_0 = B; G_1 = -i ky Q; G_2 = -i kz Q  (Q in A); layout (x, 3, n1, n2h)
         for (int it = threadIdx.x; it < N * T; it += XT) {
             const int t = it % T, x = it / T;
             const int64_t l = l0 + t;
             if (l >= g.n2h) continue;
-            const int q = Col<N, R2>::at(t, x);
-            const float qr = are[q], qi = aim[q];
+            const int q = C::at(t, x);
+            const float2 Q = A[q];
             const float mzl = __ldg(mz + l);
             float2 *o = G + ((int64_t)x * 3 * g.n1 + j) * g.n2h + l;
-            o[0] = make_float2(bre[q], bim[q]);
-            o[g.n1 * g.n2h] = make_float2(__fmul_rn(myj, qi), -__fmul_rn(myj, qr));
-            o[2 * g.n1 * g.n2h] = make_float2(__fmul_rn(mzl, qi), -__fmul_rn(mzl, qr));
+            o[0] = B[q];
+            o[g.n1 * g.n2h] = make_float2(__fmul_rn(myj, Q.y), -__fmul_rn(myj, Q.x));
+            o[2 * g.n1 * g.n2h] = make_float2(__fmul_rn(mzl, Q.y), -__fmul_rn(mzl, Q.x));
         }
     }
 }
@@ -359,10 +357,9 @@ __global__ void __launch_bounds__(XT) k_xpass_adj(const float2 *__restrict__ Cin
                                                   int64_t n0) {
     using C = XCfg<N>;
     constexpr int T = C::T, R1 = C::R1, R2 = C::R2;
-    extern __shared__ float smem[];
-    float *are = smem, *aim = smem + C::BUF;
-    float *bre = smem + 2 * C::BUF, *bim = smem + 3 * C::BUF;
-    float2 *tw = reinterpret_cast<float2 *>(smem + 4 * C::BUF);
+    extern __shared__ __align__(16) float2 smem2[];
+    float2 *A = smem2, *B = smem2 + C::BUF;
+    float2 *tw = smem2 + 2 * C::BUF;
     for (int m = threadIdx.x; m < N; m += XT) tw[m] = twg[m];
 
     const int64_t tot = n0 + g.n1 + g.n2h;
@@ -375,7 +372,7 @@ __global__ void __launch_bounds__(XT) k_xpass_adj(const float2 *__restrict__ Cin
         const float myj = __ldg(my + j);
         __syncthreads();
         // A = C_0;  B = i ky C_1 + i kz C_2   (i k (a + i b) = (-k b, k a))
-        load_tile<N>(Cin, 3, 0, j, l0, g, are, aim);
+        load_tile<N>(Cin, 3, 0, j, l0, g, A);
         {
             constexpr int PER = N * T / XT;
             constexpr int CH = PER < 8 ? PER : 8;
@@ -395,52 +392,61 @@ __global__ void __launch_bounds__(XT) k_xpass_adj(const float2 *__restrict__ Cin
                     c2[r] = ok ? __ldg(base + x * xs + 2 * cs) : make_float2(0.f, 0.f);
                 }
 #pragma unroll
-                for (int r = 0; r < CH; ++r) {
-                    const int q = Col<N, R2>::at(t, x0 + (b + r) * (XT / T));
-                    bre[q] = -__fadd_rn(__fmul_rn(myj, c1[r].y), __fmul_rn(mzl, c2[r].y));
-                    bim[q] = __fadd_rn(__fmul_rn(myj, c1[r].x), __fmul_rn(mzl, c2[r].x));
-                }
+                for (int r = 0; r < CH; ++r)
+                    B[C::at(t, x0 + (b + r) * (XT / T))] =
+                        make_float2(-__fadd_rn(__fmul_rn(myj, c1[r].y), __fmul_rn(mzl, c2[r].y)),
+                                    __fadd_rn(__fmul_rn(myj, c1[r].x), __fmul_rn(mzl, c2[r].x)));
             }
         }
         __syncthreads();
-        fft_fwd<N>(are, aim, tw);
-        fft_fwd<N>(bre, bim, tw);
+        fwd_step1<N>(A, tw);
+        fwd_step1<N>(B, tw);
+        __syncthreads();
         const float kyj = __ldg(ky + j);
         const float ky2 = __fmul_rn(kyj, kyj);
-        for (int it = threadIdx.x; it < N * T; it += XT) {
-            const int t = it / N, p = it % N;
-            const int k1 = p / R2, k2 = p % R2;
-            const int ix = k1 + R1 * k2;
+        for (int it = threadIdx.x; it < T * R1; it += XT) {
+            const int t = it / R1, k1 = it % R1;
             const int64_t l = l0 + t;
-            const float kxi = __ldg(kx + ix), mxi = __ldg(mx + ix);
             const float kzl = l < g.n2h ? __ldg(kz + l) : 0.f;
-            const float k2v = __fadd_rn(__fadd_rn(__fmul_rn(kxi, kxi), ky2), __fmul_rn(kzl, kzl));
-            const int q = Col<N, R2>::at(t, p);
-            const float re = __fadd_rn(-__fmul_rn(mxi, aim[q]), bre[q]);
-            const float im = __fadd_rn(__fmul_rn(mxi, are[q]), bim[q]);
-            float sr = 0.f, si = 0.f;
-            if (k2v != 0.f) {
-                sr = -__fdiv_rn(__fmul_rn(re, g.c), k2v);
-                si = -__fdiv_rn(__fmul_rn(im, g.c), k2v);
+            const float kz2 = __fmul_rn(kzl, kzl);
+            float2 v[R2], w[R2];
+#pragma unroll
+            for (int b = 0; b < R2; ++b) v[b] = A[C::at(t, k1 * R2 + b)];
+            dft2<R2, false>(v);
+#pragma unroll
+            for (int b = 0; b < R2; ++b) w[b] = B[C::at(t, k1 * R2 + b)];
+            dft2<R2, false>(w);
+#pragma unroll
+            for (int k = 0; k < R2; ++k) {
+                const int ix = k1 + R1 * brev(k, Log2<R2>::v);
+                const float kxi = __ldg(kx + ix), mxi = __ldg(mx + ix);
+                const float k2v = __fadd_rn(__fadd_rn(__fmul_rn(kxi, kxi), ky2), kz2);
+                const float re = __fadd_rn(-__fmul_rn(mxi, v[k].y), w[k].x);
+                const float im = __fadd_rn(__fmul_rn(mxi, v[k].x), w[k].y);
+                float sr = 0.f, si = 0.f;
+                if (k2v != 0.f) {
+                    sr = -__fdiv_rn(__fmul_rn(re, g.c), k2v);
+                    si = -__fdiv_rn(__fmul_rn(im, g.c), k2v);
+                }
+                v[k] = make_float2(sr, si);
             }
-            are[q] = sr;
-            aim[q] = si;
+            inv_step2_store<N>(v, A, t, k1, tw);
         }
         __syncthreads();
-        fft_inv<N>(are, aim, tw);
+        inv_step1<N>(A);
+        __syncthreads();
         for (int it = threadIdx.x; it < N * T; it += XT) {
             const int t = it % T, x = it / T;
             const int64_t l = l0 + t;
             if (l >= g.n2h) continue;
-            const int q = Col<N, R2>::at(t, x);
-            S[((int64_t)x * g.n1 + j) * g.n2h + l] = make_float2(are[q], aim[q]);
+            S[((int64_t)x * g.n1 + j) * g.n2h + l] = A[C::at(t, x)];
         }
     }
 }
 
 template <int N>
 size_t xpass_smem() {
-    return (size_t)4 * XCfg<N>::BUF * sizeof(float) + (size_t)N * sizeof(float2);
+    return (size_t)(2 * XCfg<N>::BUF + N) * sizeof(float2);
 }
 
 template <int N>
@@ -451,26 +457,19 @@ int launch_xpass(bool adj, const float2 *in, float2 *out, const float *kt, const
     g.n2h = n2h;
     g.ncol_tiles = (n2h + XCfg<N>::T - 1) / XCfg<N>::T;
     g.c = c;
-    size_t sm = xpass_smem<N>();
-    int64_t tiles = n1 * g.ncol_tiles;
-    int64_t cap = (int64_t)device_sms() * (sm > 110 * 1024 ? 1 : 2);
-    int grid = (int)(tiles < cap ? tiles : cap);
+    const size_t sm = xpass_smem<N>();
+    const int64_t tiles = n1 * g.ncol_tiles;
+    const int per_sm = sm > 110 * 1024 ? 1 : (sm > 72 * 1024 ? 2 : 3);
+    const int64_t cap = (int64_t)device_sms() * per_sm;
+    const int grid = (int)(tiles < cap ? tiles : cap);
     if (adj) {
-        static bool attr = false;
-        if (!attr) {
-            PMX_CUDA(cudaFuncSetAttribute(k_xpass_adj<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)sm));
-            attr = true;
-        }
+        PMX_CUDA(cudaFuncSetAttribute(k_xpass_adj<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sm));
         k_xpass_adj<N><<<grid, XT, sm, st>>>(in, out, kt, tw, g, (int64_t)N);
         PMX_LAUNCH_CHECK("k_xpass_adj");
     } else {
-        static bool attr = false;
-        if (!attr) {
-            PMX_CUDA(cudaFuncSetAttribute(k_xpass_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)sm));
-            attr = true;
-        }
+        PMX_CUDA(cudaFuncSetAttribute(k_xpass_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sm));
         k_xpass_fwd<N><<<grid, XT, sm, st>>>(in, out, kt, tw, g, (int64_t)N);
         PMX_LAUNCH_CHECK("k_xpass_fwd");
     }

@@ -357,6 +357,7 @@ constexpr size_t WIN3_SMEM = 3 * WIN1_SMEM;                           // three c
 
 struct Win {
     int x0, y0, z0;         // unwrapped origin (z0 multiple of 4)
+    int nx, ny, ng;         // rows and 4-cell groups the warp can have touched
 };
 
 __device__ __forceinline__ int warp_min(int v) {
@@ -365,14 +366,26 @@ __device__ __forceinline__ int warp_min(int v) {
     return v;
 }
 
-// Origin of the warp's window from the lower-neighbour unwrapped indices of
-// its active lanes.
+__device__ __forceinline__ int warp_max(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Origin and extent of the warp's window from the lower-neighbour unwrapped
+// indices of its active lanes (each particle also touches index + 1).
 __device__ __forceinline__ Win win_origin(bool act, const Axis ax[3]) {
     Win w;
     w.x0 = warp_min(act ? ax[0].u : INT_MAX);
     w.y0 = warp_min(act ? ax[1].u : INT_MAX);
     const int zm = warp_min(act ? ax[2].u : INT_MAX);
     w.z0 = zm & ~3;  // floor to a multiple of 4 (two's complement)
+    const int xM = warp_max(act ? ax[0].u : INT_MIN);
+    const int yM = warp_max(act ? ax[1].u : INT_MIN);
+    const int zM = warp_max(act ? ax[2].u : INT_MIN);
+    w.nx = min(3, xM - w.x0 + 2);
+    w.ny = min(3, yM - w.y0 + 2);
+    w.ng = min(WZ / 4, (zM + 1 - w.z0) / 4 + 1);
     return w;
 }
 
@@ -398,11 +411,12 @@ template <int NC>
 __device__ __forceinline__ void win_flush(float *buf, const Win &w, const Hot &h, float *base,
                                           int64_t xstride, int64_t cstride) {
     const int lane = threadIdx.x & 31;
-    constexpr int G = WZ / 4;
-    for (int idx = lane; idx < NC * WROWS * G; idx += 32) {
-        const int c = idx / (WROWS * G);
-        const int r = (idx / G) % WROWS;
-        const int g = idx % G;
+    const int ng = w.ng, nrow = w.nx * w.ny;
+    for (int idx = lane; idx < NC * nrow * ng; idx += 32) {
+        const int c = idx / (nrow * ng);
+        const int rr = (idx / ng) % nrow;
+        const int r = (rr / w.ny) * 3 + rr % w.ny;   // window row (dx * 3 + dy)
+        const int g = idx % ng;
         float4 *p = reinterpret_cast<float4 *>(buf + (c * WROWS + r) * WZ) + g;
         const float4 v = *p;
         if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
@@ -1213,7 +1227,7 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
     if (n > 0) {
         {
             Stage sg(ws, 7, s, 1);
-            k_g3adj<<<G, PT, WIN3_SMEM, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M, ws->g, ws->mcot,
+            k_g3adj<<<G, PT, h.win ? WIN3_SMEM : 0, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M, ws->g, ws->mcot,
                                      ws->part);
             PMX_LAUNCH_CHECK("k_g3adj");
         }
@@ -1404,7 +1418,7 @@ static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const 
     if ((st = force_meshes(ws, h, omega_m, s))) return st;
     {
         Stage sg(ws, 7, s, 1);
-        k_g3adj<<<G, PT, WIN3_SMEM, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M, ws->g, ws->mcot,
+        k_g3adj<<<G, PT, h.win ? WIN3_SMEM : 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M, ws->g, ws->mcot,
                                  ws->part);
         PMX_LAUNCH_CHECK("k_g3adj");
     }

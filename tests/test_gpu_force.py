@@ -293,4 +293,4 @@ def test_window_deposit_equals_direct_atomics(cuda, shuffle):
     assert rel_l2(a1, acc_o) < RTOL_ACC
     assert rel_l2(a1, a2) < 1e-6
     assert rel_l2(d1, d2) < 1e-5
-    assert abs(o1 / o2 - 1) < 1e-6
+    assert abs(o1 / o2 - 1) < 5e-5   # a float64 sum over ~1e5 float32 terms in any order
