@@ -112,9 +112,14 @@ typedef struct pmx_workspace pmx_workspace;
 #define PMX_WS_CUFFT3D 2   /* use 3-D cuFFT plans even where the fused x pass
                               applies (n0 a power of two in 64..1024);
                               for comparisons and tests */
-#define PMX_WS_NO_WINDOW 4 /* deposit with one global atomic per contribution
-                              instead of per-warp shared-memory windows
-                              flushed with 16-byte vector reductions */
+#define PMX_WS_WINDOW 4    /* deposit through per-warp shared-memory windows
+                              flushed with 16-byte vector reductions instead
+                              of one global atomic per contribution (opt-in:
+                              slower for lattice-ordered particles on GB300) */
+#define PMX_WS_PLANE 8     /* with the fused x pass, do the (y, z) plane
+                              transforms with the cluster plane kernels
+                              instead of slab-wise 2-D cuFFT (square
+                              power-of-two planes 64..1024) */
 
 /* Device bytes a workspace for this 3-D mesh allocates (meshes, spectra,
  * cuFFT work areas, reduction scratch). */

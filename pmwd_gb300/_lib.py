@@ -84,7 +84,8 @@ def profile_read(ws):
 
 PMX_WS_ADJOINT = 1
 PMX_WS_CUFFT3D = 2
-PMX_WS_NO_WINDOW = 4
+PMX_WS_WINDOW = 4
+PMX_WS_PLANE = 8
 
 _lib = None
 _lock = threading.Lock()
@@ -160,12 +161,13 @@ def make_spec(dim, wrap_shape, mesh_shape, conf_cell_size, offset=0, cell_size=N
 class Workspace:
     """Owner of a ``pmx_workspace`` (mesh buffers, spectra, cuFFT plans)."""
 
-    def __init__(self, mesh_shape, adjoint=True, device=None, cufft3d=False, window=True):
+    def __init__(self, mesh_shape, adjoint=True, device=None, cufft3d=False, window=False,
+                 plane=False):
         load()
         self.mesh_shape = tuple(int(s) for s in mesh_shape)
         self.adjoint = adjoint
         flags = ((PMX_WS_ADJOINT if adjoint else 0) | (PMX_WS_CUFFT3D if cufft3d else 0)
-                 | (0 if window else PMX_WS_NO_WINDOW))
+                 | (PMX_WS_WINDOW if window else 0) | (PMX_WS_PLANE if plane else 0))
         self.device = torch.device('cuda', torch.cuda.current_device() if device is None else device)
         shp = (c_i64 * 3)(*self.mesh_shape)
         h = c_p()

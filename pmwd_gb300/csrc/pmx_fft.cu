@@ -26,6 +26,7 @@
 // of R2 values, so one thread does them back to back in registers; the
 // spectrum never needs natural order and no reordering pass exists.
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -71,8 +72,6 @@ struct Twiddle32 {
     }
 };
 
-__constant__ Twiddle32 c_tw32 = Twiddle32();
-
 template <int R>
 struct Log2 {
     static constexpr int v = R <= 1 ? 0 : 1 + Log2<R / 2>::v;
@@ -87,6 +86,8 @@ struct Log2<1> {
 // decimation in frequency.  The butterflies are generated by fold
 // expressions so every register index is a compile-time constant (the
 // arrays stay in registers).  INV selects exp(+2 pi i ...) (unnormalised).
+constexpr Twiddle32 kTw32 = Twiddle32();
+
 template <int R, bool INV, int S, int J>
 __device__ __forceinline__ void bfly(float (&re)[R], float (&im)[R]) {
     constexpr int half = 1 << (S - 1), len = 1 << S;
@@ -96,10 +97,19 @@ __device__ __forceinline__ void bfly(float (&re)[R], float (&im)[R]) {
     re[a] = ur + vr;
     im[a] = ui + vi;
     const float dr = ur - vr, di = ui - vi;
-    const float wc = c_tw32.c[ti];
-    const float ws = INV ? c_tw32.s[ti] : -c_tw32.s[ti];
-    re[b] = dr * wc - di * ws;
-    im[b] = dr * ws + di * wc;
+    // twiddle exp(-+2 pi i ti / 32), a compile-time constant; 1 and -+i exactly
+    if constexpr (ti == 0) {
+        re[b] = dr;
+        im[b] = di;
+    } else if constexpr (ti == 8) {
+        re[b] = INV ? -di : di;
+        im[b] = INV ? dr : -dr;
+    } else {
+        constexpr float wc = kTw32.c[ti];
+        constexpr float ws = INV ? kTw32.s[ti] : -kTw32.s[ti];
+        re[b] = dr * wc - di * ws;
+        im[b] = dr * ws + di * wc;
+    }
 }
 
 template <int R, bool INV, int S, int... Js>
@@ -163,79 +173,107 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a * conj(b)
 
 template <int N>
 struct Split;  // N = R1 * R2
+template <> struct Split<32> { static constexpr int R1 = 8, R2 = 4; };
 template <> struct Split<64> { static constexpr int R1 = 8, R2 = 8; };
 template <> struct Split<128> { static constexpr int R1 = 16, R2 = 8; };
 template <> struct Split<256> { static constexpr int R1 = 16, R2 = 16; };
 template <> struct Split<512> { static constexpr int R1 = 32, R2 = 16; };
 template <> struct Split<1024> { static constexpr int R1 = 32, R2 = 32; };
 
-constexpr int XT = 256;  // threads per x-pass CTA
+constexpr int XTF = 256;  // threads per forward x-pass CTA
+constexpr int XTA = 256;  // threads per adjoint x-pass CTA
 
-// Column buffers of complex (float2) values: column t at t*CS, logical
-// position p at p + p/R2 (one pad per R2 values keeps the strided and the
-// contiguous DFT steps free of bank conflicts for 8-byte accesses; the +1
-// per column does the same for the tile loads and stores).
-template <int N>
+// Column stride of the padded tile buffers.  One pad per R2 values keeps the
+// strided and the contiguous DFT steps free of bank conflicts for 8-byte
+// accesses.  The tile loads and stores walk (column t, row x) with t fastest;
+// 16 lanes (one 128-byte wavefront) then cover T columns x 16/T rows, which
+// hit 16 distinct bank pairs when CS = 16/T (mod 16) for T <= 16, or CS odd.
+constexpr int pad_cs(int n, int r2, int t) {
+    int cs = n + n / r2 + 1;
+    if (t > 16) return cs | 1;
+    while (cs % 16 != 16 / t) ++cs;
+    return cs;
+}
+
+// Tile geometry: T columns (fixed ky, consecutive kz) of length N, column t
+// at t*CS, logical position p at p + p/R2.
+template <int N, int XTH>
 struct XCfg {
+    static constexpr int TH = XTH;
     static constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2;
     static constexpr int RM = R1 > R2 ? R1 : R2;
-    static constexpr int T = XT / RM;  // columns per CTA
-    static constexpr int CS = N + N / R2 + 1;
+    static constexpr int T = XTH / RM;  // columns per CTA
+    static constexpr int CS = pad_cs(N, R2, T);
     static constexpr int BUF = T * CS;  // float2 per buffer
+    static constexpr int PER = N * T / XTH;  // tile elements per thread
     __device__ static __forceinline__ int at(int t, int p) { return t * CS + p + p / R2; }
 };
 
+// 8-byte asynchronous global -> shared copy; ok == false writes zeros and
+// reads nothing (src must still be a valid address).
+__device__ __forceinline__ void cp_async8(float2 *dst, const float2 *src, bool ok) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int n = ok ? 8 : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(n)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_group1() {
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+}
+
 // Forward step 1 on one buffer: R2-strided radix-R1 DFTs + twiddles,
 // natural order -> "transposed" positions k1*R2 + b.
-template <int N>
+template <class C>
 __device__ __forceinline__ void fwd_step1(float2 *buf, const float2 *tw) {
-    using C = XCfg<N>;
     constexpr int R1 = C::R1, R2 = C::R2;
-    for (int it = threadIdx.x; it < C::T * R2; it += XT) {
+    for (int it = threadIdx.x; it < C::T * R2; it += C::TH) {
         const int t = it / R2, b = it % R2;
+        float2 *col = buf + t * C::CS + b;  // position a*R2 + b at col[a*(R2+1)]
         float2 v[R1];
 #pragma unroll
-        for (int a = 0; a < R1; ++a) v[a] = buf[C::at(t, a * R2 + b)];
+        for (int a = 0; a < R1; ++a) v[a] = col[a * (R2 + 1)];
         dft2<R1, false>(v);
 #pragma unroll
         for (int k = 0; k < R1; ++k) {
             const int k1 = brev(k, Log2<R1>::v);
-            buf[C::at(t, k1 * R2 + b)] = cmul(v[k], tw[b * k1]);
+            col[k1 * (R2 + 1)] = cmul(v[k], tw[b * k1]);
         }
     }
 }
 
 // Inverse step 1 (the last inverse step) on one buffer: radix-R1 inverse
 // DFTs over k1 at fixed b -> natural order.
-template <int N>
+template <class C>
 __device__ __forceinline__ void inv_step1(float2 *buf) {
-    using C = XCfg<N>;
     constexpr int R1 = C::R1, R2 = C::R2;
-    for (int it = threadIdx.x; it < C::T * R2; it += XT) {
+    for (int it = threadIdx.x; it < C::T * R2; it += C::TH) {
         const int t = it / R2, b = it % R2;
+        float2 *col = buf + t * C::CS + b;
         float2 v[R1];
 #pragma unroll
-        for (int k1 = 0; k1 < R1; ++k1) v[k1] = buf[C::at(t, k1 * R2 + b)];
+        for (int k1 = 0; k1 < R1; ++k1) v[k1] = col[k1 * (R2 + 1)];
         dft2<R1, true>(v);
 #pragma unroll
-        for (int k = 0; k < R1; ++k) buf[C::at(t, brev(k, Log2<R1>::v) * R2 + b)] = v[k];
+        for (int k = 0; k < R1; ++k) col[brev(k, Log2<R1>::v) * (R2 + 1)] = v[k];
     }
 }
 
 // Inverse step 2 on a register group in bit-reversed k2 order (as the
 // forward step 2 leaves it), twiddle, store to positions k1*R2 + b.
-template <int N>
-__device__ __forceinline__ void inv_step2_store(float2 (&v)[XCfg<N>::R2], float2 *buf, int t,
-                                                int k1, const float2 *tw) {
-    using C = XCfg<N>;
+template <class C>
+__device__ __forceinline__ void inv_step2_store(float2 (&v)[C::R2], float2 *buf, int t, int k1,
+                                                const float2 *tw) {
     constexpr int R2 = C::R2;
     float2 u[R2];
     unbrev<R2>(v, u);           // natural k2 order
     dft2<R2, true>(u);          // element k holds b = brev(k)
+    float2 *grp = buf + t * C::CS + k1 * (R2 + 1);  // position k1*R2 + b at grp[b]
 #pragma unroll
     for (int k = 0; k < R2; ++k) {
         const int b = brev(k, Log2<R2>::v);
-        buf[C::at(t, k1 * R2 + b)] = cmulc(u[k], tw[b * k1]);
+        grp[b] = cmulc(u[k], tw[b * k1]);
     }
 }
 
@@ -245,208 +283,248 @@ struct XGeom {
     float c;              // 1.5 Omega_m / N
 };
 
-// Loads the column tile (fixed ky row j, kz in [l0, l0+T), all x) of a
-// complex array laid out (x, ncomp, n1, n2h), component `comp`; optionally
-// combines two components: out = (i k1m) in1 + (i k2m) in2.
-template <int N>
-__device__ __forceinline__ void load_tile(const float2 *__restrict__ src, int ncomp, int comp,
-                                          int64_t j, int64_t l0, const XGeom &g, float2 *buf) {
-    using C = XCfg<N>;
-    constexpr int T = C::T;
-    constexpr int PER = N * T / XT;
-    constexpr int CH = PER < 16 ? PER : 16;
-    const int t = threadIdx.x % T;
-    const int x0 = threadIdx.x / T;
+// Starts the asynchronous load of the column tile (fixed ky row j, kz in
+// [l0, l0+T), all x) of component `comp` of a complex array laid out
+// (x, ncomp, n1, n2h); columns past n2h read as zero.
+template <class C>
+__device__ __forceinline__ void issue_tile(const float2 *__restrict__ src, int ncomp, int comp,
+                                           int64_t j, int64_t l0, const XGeom &g, float2 *buf) {
+    constexpr int T = C::T, XS = C::TH / C::T;
+    const int t = threadIdx.x % T, x0 = threadIdx.x / T;
     const int64_t l = l0 + t;
     const bool ok = l < g.n2h;
-    const float2 *base = src + ((int64_t)comp * g.n1 + j) * g.n2h + l;
+    const float2 *base = src + ((int64_t)comp * g.n1 + j) * g.n2h + (ok ? l : 0);
     const int64_t xs = (int64_t)ncomp * g.n1 * g.n2h;
-#pragma unroll
-    for (int b = 0; b < PER; b += CH) {
-        float2 v[CH];
-#pragma unroll
-        for (int r = 0; r < CH; ++r) {
-            const int x = x0 + (b + r) * (XT / T);
-            v[r] = ok ? __ldg(base + x * xs) : make_float2(0.f, 0.f);
-        }
-#pragma unroll
-        for (int r = 0; r < CH; ++r) buf[C::at(t, x0 + (b + r) * (XT / T))] = v[r];
+#pragma unroll 8
+    for (int r = 0; r < C::PER; ++r) {
+        const int x = x0 + r * XS;
+        cp_async8(buf + C::at(t, x), base + x * xs, ok);
     }
 }
 
+// Both kernels are software pipelined: while a CTA transforms one tile, the
+// cp.async copies of its next tile are in flight into a second buffer set,
+// so the HBM reads overlap the shared-memory FFT work and the stores.
+
 template <int N>
-__global__ void __launch_bounds__(XT) k_xpass_fwd(const float2 *__restrict__ H,
-                                                  float2 *__restrict__ G,
-                                                  const float *__restrict__ kt,
-                                                  const float2 *__restrict__ twg, XGeom g,
-                                                  int64_t n0) {
-    using C = XCfg<N>;
+__global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__ H,
+                                                      float2 *__restrict__ G,
+                                                      const float *__restrict__ kt,
+                                                      const float2 *__restrict__ twg, XGeom g,
+                                                      int64_t n0) {
+    using C = XCfg<N, XTF>;
     constexpr int T = C::T, R1 = C::R1, R2 = C::R2;
     extern __shared__ __align__(16) float2 smem2[];
-    float2 *A = smem2, *B = smem2 + C::BUF;
-    float2 *tw = smem2 + 2 * C::BUF;
-    for (int m = threadIdx.x; m < N; m += XT) tw[m] = twg[m];
+    float2 *A0 = smem2, *A1 = smem2 + C::BUF, *B = smem2 + 2 * C::BUF;
+    float2 *tw = smem2 + 3 * C::BUF;
+    float *kxs = reinterpret_cast<float *>(tw + N), *mxs = kxs + N;
 
     const int64_t tot = n0 + g.n1 + g.n2h;
-    const float *kx = kt, *ky = kt + n0, *kz = kt + n0 + g.n1;
-    const float *mx = kt + tot, *my = kt + tot + n0, *mz = kt + tot + n0 + g.n1;
+    const float *ky = kt + n0, *kz = kt + n0 + g.n1;
+    const float *my = kt + tot + n0, *mz = kt + tot + n0 + g.n1;
+    for (int m = threadIdx.x; m < N; m += XTF) {
+        tw[m] = twg[m];
+        kxs[m] = kt[m];
+        mxs[m] = kt[tot + m];
+    }
 
-    for (int64_t tile = blockIdx.x; tile < g.n1 * g.ncol_tiles; tile += gridDim.x) {
+    const int64_t ntiles = g.n1 * g.ncol_tiles;
+    int64_t tile = blockIdx.x;
+    if (tile < ntiles)
+        issue_tile<C>(H, 1, 0, tile / g.ncol_tiles, (tile % g.ncol_tiles) * T, g, A0);
+    cp_async_commit();
+    for (int cur = 0; tile < ntiles; tile += gridDim.x, cur ^= 1) {
+        float2 *A = cur ? A1 : A0;
         const int64_t j = tile / g.ncol_tiles;
         const int64_t l0 = (tile % g.ncol_tiles) * T;
-        __syncthreads();  // buffers free (also orders the twiddle fill)
-        load_tile<N>(H, 1, 0, j, l0, g, A);
+        cp_async_wait_all();
+        // this tile is in A; the previous tile's store phase (reads of the
+        // other A buffer and of B) is over; the tables are filled
         __syncthreads();
-        fwd_step1<N>(A, tw);
+        const int64_t nxt = tile + gridDim.x;
+        if (nxt < ntiles)
+            issue_tile<C>(H, 1, 0, nxt / g.ncol_tiles, (nxt % g.ncol_tiles) * T, g, cur ? A0 : A1);
+        cp_async_commit();
+        fwd_step1<C>(A, tw);
         __syncthreads();
         // fused: forward step 2, Green + gradient, inverse step 2 of P and of
         // B = -i kx P, all on one thread's contiguous group
         const float kyj = __ldg(ky + j), myj = __ldg(my + j);
         const float ky2 = __fmul_rn(kyj, kyj);
-        for (int it = threadIdx.x; it < T * R1; it += XT) {
+        for (int it = threadIdx.x; it < T * R1; it += XTF) {
             const int t = it / R1, k1 = it % R1;
             const int64_t l = l0 + t;
             const float kzl = l < g.n2h ? __ldg(kz + l) : 0.f;
             const float kz2 = __fmul_rn(kzl, kzl);
             float2 v[R2];
 #pragma unroll
-            for (int b = 0; b < R2; ++b) v[b] = A[C::at(t, k1 * R2 + b)];
+            for (int b = 0; b < R2; ++b) v[b] = A[t * C::CS + k1 * (R2 + 1) + b];
             dft2<R2, false>(v);          // element k: kx index k1 + R1*brev(k)
             float2 w[R2];
 #pragma unroll
             for (int k = 0; k < R2; ++k) {
                 const int ix = k1 + R1 * brev(k, Log2<R2>::v);
-                const float kxi = __ldg(kx + ix), mxi = __ldg(mx + ix);
+                const float kxi = kxs[ix], mxi = mxs[ix];
                 const float k2v = __fadd_rn(__fadd_rn(__fmul_rn(kxi, kxi), ky2), kz2);
-                float pr = 0.f, pi = 0.f;
-                if (k2v != 0.f) {
-                    pr = -__fdiv_rn(__fmul_rn(v[k].x, g.c), k2v);
-                    pi = -__fdiv_rn(__fmul_rn(v[k].y, g.c), k2v);
-                }
+                // laplace (k = 0 -> 0); c / k^2 to within 2 ulp
+                const float rk = k2v != 0.f ? __fdividef(g.c, k2v) : 0.f;
+                const float pr = -__fmul_rn(v[k].x, rk), pi = -__fmul_rn(v[k].y, rk);
                 v[k] = make_float2(pr, pi);
                 w[k] = make_float2(__fmul_rn(mxi, pi), -__fmul_rn(mxi, pr));  // -i kx P
             }
-            inv_step2_store<N>(v, A, t, k1, tw);
-            inv_step2_store<N>(w, B, t, k1, tw);
+            inv_step2_store<C>(v, A, t, k1, tw);
+            inv_step2_store<C>(w, B, t, k1, tw);
         }
         __syncthreads();
-        inv_step1<N>(A);
-        inv_step1<N>(B);
+        inv_step1<C>(A);
+        inv_step1<C>(B);
         __syncthreads();
         // G_0 = B; G_1 = -i ky Q; G_2 = -i kz Q  (Q in A); layout (x, 3, n1, n2h)
-        for (int it = threadIdx.x; it < N * T; it += XT) {
-            const int t = it % T, x = it / T;
+        {
+            constexpr int XS = XTF / T;
+            const int t = threadIdx.x % T;
             const int64_t l = l0 + t;
-            if (l >= g.n2h) continue;
-            const int q = C::at(t, x);
-            const float2 Q = A[q];
-            const float mzl = __ldg(mz + l);
-            float2 *o = G + ((int64_t)x * 3 * g.n1 + j) * g.n2h + l;
-            o[0] = B[q];
-            o[g.n1 * g.n2h] = make_float2(__fmul_rn(myj, Q.y), -__fmul_rn(myj, Q.x));
-            o[2 * g.n1 * g.n2h] = make_float2(__fmul_rn(mzl, Q.y), -__fmul_rn(mzl, Q.x));
+            if (l < g.n2h) {
+                const float mzl = __ldg(mz + l);
+                const int64_t cs = g.n1 * g.n2h, xs = 3 * cs;
+                float2 *o = G + j * g.n2h + l;
+                for (int x = threadIdx.x / T; x < N; x += XS) {
+                    const int q = C::at(t, x);
+                    const float2 Q = A[q];
+                    float2 *ox = o + x * xs;
+                    ox[0] = B[q];
+                    ox[cs] = make_float2(__fmul_rn(myj, Q.y), -__fmul_rn(myj, Q.x));
+                    ox[2 * cs] = make_float2(__fmul_rn(mzl, Q.y), -__fmul_rn(mzl, Q.x));
+                }
+            }
         }
+    }
+    cp_async_wait_all();
+}
+
+// Loads B = i ky C_1 + i kz C_2 of a column tile (components 1, 2 of the
+// (x, 3, n1, n2h) array) synchronously, in register batches.
+template <class C>
+__device__ __forceinline__ void load_comb(const float2 *__restrict__ Cin, int64_t j, int64_t l0,
+                                          float myj, const float *__restrict__ mz,
+                                          const XGeom &g, float2 *buf) {
+    constexpr int T = C::T, XS = C::TH / C::T, PER = C::PER, CH = PER < 8 ? PER : 8;
+    const int t = threadIdx.x % T, x0 = threadIdx.x / T;
+    const int64_t l = l0 + t;
+    const bool ok = l < g.n2h;
+    const float mzl = ok ? __ldg(mz + l) : 0.f;
+    const int64_t cs = g.n1 * g.n2h, xs = 3 * cs;
+    const float2 *base = Cin + j * g.n2h + (ok ? l : 0);
+#pragma unroll
+    for (int b = 0; b < PER; b += CH) {
+        float2 c1[CH], c2[CH];
+#pragma unroll
+        for (int r = 0; r < CH; ++r) {
+            const int x = x0 + (b + r) * XS;
+            c1[r] = ok ? __ldg(base + x * xs + cs) : make_float2(0.f, 0.f);
+            c2[r] = ok ? __ldg(base + x * xs + 2 * cs) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int r = 0; r < CH; ++r)  // i k (a + i b) = (-k b, k a)
+            buf[C::at(t, x0 + (b + r) * XS)] =
+                make_float2(-__fadd_rn(__fmul_rn(myj, c1[r].y), __fmul_rn(mzl, c2[r].y)),
+                            __fadd_rn(__fmul_rn(myj, c1[r].x), __fmul_rn(mzl, c2[r].x)));
     }
 }
 
 template <int N>
-__global__ void __launch_bounds__(XT) k_xpass_adj(const float2 *__restrict__ Cin,
-                                                  float2 *__restrict__ S,
-                                                  const float *__restrict__ kt,
-                                                  const float2 *__restrict__ twg, XGeom g,
-                                                  int64_t n0) {
-    using C = XCfg<N>;
+__global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__ Cin,
+                                                      float2 *__restrict__ S,
+                                                      const float *__restrict__ kt,
+                                                      const float2 *__restrict__ twg, XGeom g,
+                                                      int64_t n0) {
+    using C = XCfg<N, XTA>;
     constexpr int T = C::T, R1 = C::R1, R2 = C::R2;
     extern __shared__ __align__(16) float2 smem2[];
-    float2 *A = smem2, *B = smem2 + C::BUF;
-    float2 *tw = smem2 + 2 * C::BUF;
-    for (int m = threadIdx.x; m < N; m += XT) tw[m] = twg[m];
+    float2 *A0 = smem2, *A1 = smem2 + C::BUF, *B = smem2 + 2 * C::BUF;
+    float2 *tw = smem2 + 3 * C::BUF;
+    float *kxs = reinterpret_cast<float *>(tw + N), *mxs = kxs + N;
 
     const int64_t tot = n0 + g.n1 + g.n2h;
-    const float *kx = kt, *ky = kt + n0, *kz = kt + n0 + g.n1;
-    const float *mx = kt + tot, *my = kt + tot + n0, *mz = kt + tot + n0 + g.n1;
+    const float *ky = kt + n0, *kz = kt + n0 + g.n1;
+    const float *my = kt + tot + n0, *mz = kt + tot + n0 + g.n1;
+    for (int m = threadIdx.x; m < N; m += XTA) {
+        tw[m] = twg[m];
+        kxs[m] = kt[m];
+        mxs[m] = kt[tot + m];
+    }
 
-    for (int64_t tile = blockIdx.x; tile < g.n1 * g.ncol_tiles; tile += gridDim.x) {
+    const int64_t ntiles = g.n1 * g.ncol_tiles;
+    int64_t tile = blockIdx.x;
+    if (tile < ntiles)
+        issue_tile<C>(Cin, 3, 0, tile / g.ncol_tiles, (tile % g.ncol_tiles) * T, g, A0);
+    cp_async_commit();
+    for (int cur = 0; tile < ntiles; tile += gridDim.x, cur ^= 1) {
+        float2 *A = cur ? A1 : A0;
         const int64_t j = tile / g.ncol_tiles;
         const int64_t l0 = (tile % g.ncol_tiles) * T;
+        // the previous tile's store phase (reads of the other A buffer) is over
+        __syncthreads();
+        const int64_t nxt = tile + gridDim.x;
+        if (nxt < ntiles)
+            issue_tile<C>(Cin, 3, 0, nxt / g.ncol_tiles, (nxt % g.ncol_tiles) * T, g, cur ? A0 : A1);
+        cp_async_commit();
         const float myj = __ldg(my + j);
+        load_comb<C>(Cin, j, l0, myj, mz, g, B);
+        cp_async_wait_group1();  // this tile's C_0 (the next tile's may stay in flight)
         __syncthreads();
-        // A = C_0;  B = i ky C_1 + i kz C_2   (i k (a + i b) = (-k b, k a))
-        load_tile<N>(Cin, 3, 0, j, l0, g, A);
-        {
-            constexpr int PER = N * T / XT;
-            constexpr int CH = PER < 8 ? PER : 8;
-            const int t = threadIdx.x % T, x0 = threadIdx.x / T;
-            const int64_t l = l0 + t;
-            const bool ok = l < g.n2h;
-            const float mzl = ok ? __ldg(mz + l) : 0.f;
-            const int64_t cs = g.n1 * g.n2h, xs = 3 * cs;
-            const float2 *base = Cin + j * g.n2h + l;
-#pragma unroll
-            for (int b = 0; b < PER; b += CH) {
-                float2 c1[CH], c2[CH];
-#pragma unroll
-                for (int r = 0; r < CH; ++r) {
-                    const int x = x0 + (b + r) * (XT / T);
-                    c1[r] = ok ? __ldg(base + x * xs + cs) : make_float2(0.f, 0.f);
-                    c2[r] = ok ? __ldg(base + x * xs + 2 * cs) : make_float2(0.f, 0.f);
-                }
-#pragma unroll
-                for (int r = 0; r < CH; ++r)
-                    B[C::at(t, x0 + (b + r) * (XT / T))] =
-                        make_float2(-__fadd_rn(__fmul_rn(myj, c1[r].y), __fmul_rn(mzl, c2[r].y)),
-                                    __fadd_rn(__fmul_rn(myj, c1[r].x), __fmul_rn(mzl, c2[r].x)));
-            }
-        }
-        __syncthreads();
-        fwd_step1<N>(A, tw);
-        fwd_step1<N>(B, tw);
+        fwd_step1<C>(A, tw);
+        fwd_step1<C>(B, tw);
         __syncthreads();
         const float kyj = __ldg(ky + j);
         const float ky2 = __fmul_rn(kyj, kyj);
-        for (int it = threadIdx.x; it < T * R1; it += XT) {
+        for (int it = threadIdx.x; it < T * R1; it += XTA) {
             const int t = it / R1, k1 = it % R1;
             const int64_t l = l0 + t;
             const float kzl = l < g.n2h ? __ldg(kz + l) : 0.f;
             const float kz2 = __fmul_rn(kzl, kzl);
             float2 v[R2], w[R2];
 #pragma unroll
-            for (int b = 0; b < R2; ++b) v[b] = A[C::at(t, k1 * R2 + b)];
+            for (int b = 0; b < R2; ++b) v[b] = A[t * C::CS + k1 * (R2 + 1) + b];
             dft2<R2, false>(v);
 #pragma unroll
-            for (int b = 0; b < R2; ++b) w[b] = B[C::at(t, k1 * R2 + b)];
+            for (int b = 0; b < R2; ++b) w[b] = B[t * C::CS + k1 * (R2 + 1) + b];
             dft2<R2, false>(w);
 #pragma unroll
             for (int k = 0; k < R2; ++k) {
                 const int ix = k1 + R1 * brev(k, Log2<R2>::v);
-                const float kxi = __ldg(kx + ix), mxi = __ldg(mx + ix);
+                const float kxi = kxs[ix], mxi = mxs[ix];
                 const float k2v = __fadd_rn(__fadd_rn(__fmul_rn(kxi, kxi), ky2), kz2);
                 const float re = __fadd_rn(-__fmul_rn(mxi, v[k].y), w[k].x);
                 const float im = __fadd_rn(__fmul_rn(mxi, v[k].x), w[k].y);
-                float sr = 0.f, si = 0.f;
-                if (k2v != 0.f) {
-                    sr = -__fdiv_rn(__fmul_rn(re, g.c), k2v);
-                    si = -__fdiv_rn(__fmul_rn(im, g.c), k2v);
-                }
-                v[k] = make_float2(sr, si);
+                const float rk = k2v != 0.f ? __fdividef(g.c, k2v) : 0.f;
+                v[k] = make_float2(-__fmul_rn(re, rk), -__fmul_rn(im, rk));
             }
-            inv_step2_store<N>(v, A, t, k1, tw);
+            inv_step2_store<C>(v, A, t, k1, tw);
         }
         __syncthreads();
-        inv_step1<N>(A);
+        inv_step1<C>(A);
         __syncthreads();
-        for (int it = threadIdx.x; it < N * T; it += XT) {
-            const int t = it % T, x = it / T;
+        {
+            constexpr int XS = XTA / T;
+            const int t = threadIdx.x % T;
             const int64_t l = l0 + t;
-            if (l >= g.n2h) continue;
-            S[((int64_t)x * g.n1 + j) * g.n2h + l] = A[C::at(t, x)];
+            if (l < g.n2h) {
+                float2 *o = S + j * g.n2h + l;
+                const int64_t xs = g.n1 * g.n2h;
+                for (int x = threadIdx.x / T; x < N; x += XS) o[x * xs] = A[C::at(t, x)];
+            }
         }
     }
+    cp_async_wait_all();
 }
 
 template <int N>
-size_t xpass_smem() {
-    return (size_t)(2 * XCfg<N>::BUF + N) * sizeof(float2);
+size_t xpass_smem(bool adj) {
+    using CF = XCfg<N, XTF>;
+    using CA = XCfg<N, XTA>;
+    const size_t tables = (size_t)N * (sizeof(float2) + 2 * sizeof(float));
+    return (size_t)3 * (adj ? CA::BUF : CF::BUF) * sizeof(float2) + tables;
 }
 
 template <int N>
@@ -455,23 +533,322 @@ int launch_xpass(bool adj, const float2 *in, float2 *out, const float *kt, const
     XGeom g;
     g.n1 = n1;
     g.n2h = n2h;
-    g.ncol_tiles = (n2h + XCfg<N>::T - 1) / XCfg<N>::T;
     g.c = c;
-    const size_t sm = xpass_smem<N>();
+    const size_t sm = xpass_smem<N>(adj);
+    const void *fn = adj ? (const void *)k_xpass_adj<N> : (const void *)k_xpass_fwd<N>;
+    const int threads = adj ? XTA : XTF;
+    const int T = adj ? XCfg<N, XTA>::T : XCfg<N, XTF>::T;
+    g.ncol_tiles = (n2h + T - 1) / T;
+    PMX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    int per_sm = 0;
+    PMX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, sm));
+    if (per_sm < 1) return fail(PMX_ERR_CUDA, "x-pass kernel does not fit on an SM");
     const int64_t tiles = n1 * g.ncol_tiles;
-    const int per_sm = sm > 110 * 1024 ? 1 : (sm > 72 * 1024 ? 2 : 3);
     const int64_t cap = (int64_t)device_sms() * per_sm;
     const int grid = (int)(tiles < cap ? tiles : cap);
     if (adj) {
-        PMX_CUDA(cudaFuncSetAttribute(k_xpass_adj<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sm));
-        k_xpass_adj<N><<<grid, XT, sm, st>>>(in, out, kt, tw, g, (int64_t)N);
+        k_xpass_adj<N><<<grid, XTA, sm, st>>>(in, out, kt, tw, g, (int64_t)N);
         PMX_LAUNCH_CHECK("k_xpass_adj");
     } else {
-        PMX_CUDA(cudaFuncSetAttribute(k_xpass_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sm));
-        k_xpass_fwd<N><<<grid, XT, sm, st>>>(in, out, kt, tw, g, (int64_t)N);
+        k_xpass_fwd<N><<<grid, XTF, sm, st>>>(in, out, kt, tw, g, (int64_t)N);
         PMX_LAUNCH_CHECK("k_xpass_fwd");
+    }
+    return PMX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Plane (y, z) transforms.  The 3-D r2c / c2r transforms of the force are
+// the x pass above plus, per x-plane (and component), a 2-D transform over
+// (y, z): real rows of n2 values along z (contiguous) and complex columns of
+// n1 values along y (stride n2h).  One thread-block cluster of PCL CTAs owns
+// a plane at a time: each CTA transforms n1/PCL rows, the cluster
+// synchronises (barrier.cluster: release/acquire at cluster scope, so the
+// rows written by the other CTAs are visible), then each CTA transforms
+// every PCL-th tile of T columns in place.  Between the two phases the plane
+// (n1 * n2h * 8 bytes, 4.2 MB at 1024^2) sits in L2, so HBM sees one read
+// of the input and one write of the output per plane.
+//
+// Rows use the half-length complex FFT: z[m] = x[2m] + i x[2m+1],
+// Z = FFT_L(z) (L = n2/2), then X[k] = E[k] + w_N^k O[k] with
+// E[k] = (Z[k] + conj Z[L-k]) / 2, O[k] = (Z[k] - conj Z[L-k]) / 2i.  The
+// inverse rebuilds Zc[k] = (X[k] + conj X[L-k]) + i w_N^-k (X[k] - conj X[L-k])
+// (imaginary parts of X[0] and X[L] ignored, as c2r does) and z = IFFT_L(Zc).
+// All transforms are unnormalised, like cuFFT's.
+// ---------------------------------------------------------------------------
+
+namespace cg = cooperative_groups;
+
+constexpr int PTH = 256;  // threads per plane CTA
+constexpr int PCL = 8;    // CTAs per plane cluster
+
+// Length-N FFT (N = R1 * R2) of the T columns of a padded tile buffer, in
+// place, natural order in and out; INV selects exp(+2 pi i ...).  Step 2
+// gives each thread exactly one group (T * R1 == threads), which lets the
+// reordering to natural order happen in place after a barrier.
+template <class C, bool INV>
+__device__ __forceinline__ void fft_cols(float2 *buf, const float2 *tw) {
+    constexpr int R1 = C::R1, R2 = C::R2;
+    static_assert(C::T * R1 == C::TH, "one step-2 group per thread");
+    for (int it = threadIdx.x; it < C::T * R2; it += C::TH) {
+        const int t = it / R2, b = it % R2;
+        float2 *col = buf + t * C::CS + b;
+        float2 v[R1];
+#pragma unroll
+        for (int a = 0; a < R1; ++a) v[a] = col[a * (R2 + 1)];
+        dft2<R1, INV>(v);
+#pragma unroll
+        for (int k = 0; k < R1; ++k) {
+            const int k1 = brev(k, Log2<R1>::v);
+            col[k1 * (R2 + 1)] = INV ? cmulc(v[k], tw[b * k1]) : cmul(v[k], tw[b * k1]);
+        }
+    }
+    __syncthreads();
+    const int t = threadIdx.x / R1, k1 = threadIdx.x % R1;
+    float2 v[R2];
+    const float2 *grp = buf + t * C::CS + k1 * (R2 + 1);
+#pragma unroll
+    for (int b = 0; b < R2; ++b) v[b] = grp[b];
+    dft2<R2, INV>(v);  // element k: frequency k1 + R1 * brev(k)
+    __syncthreads();
+    // natural position f = k1 + R1 k2 at t*CS + k1 + k1/R2 + k2 (R1 + R1/R2)
+    float2 *nat = buf + t * C::CS + k1 + k1 / R2;
+#pragma unroll
+    for (int k = 0; k < R2; ++k) nat[brev(k, Log2<R2>::v) * (R1 + R1 / R2)] = v[k];
+    __syncthreads();
+}
+
+// Asynchronous load of T columns [l0, l0+T) (those < ncol valid, the rest
+// zero) of `rows` rows with row stride `rs` (float2) into a tile buffer.
+template <class C, int ROWS>
+__device__ __forceinline__ void issue_cols(const float2 *src, int64_t rs, int l0, int ncol,
+                                           float2 *buf) {
+    constexpr int T = C::T, XS = C::TH / C::T;
+    const int t = threadIdx.x % T, y0 = threadIdx.x / T;
+    const bool ok = l0 + t < ncol;
+    const float2 *base = src + (ok ? l0 + t : 0);
+#pragma unroll 8
+    for (int r = 0; r < ROWS / XS; ++r) {
+        const int y = y0 + r * XS;
+        cp_async8(buf + C::at(t, y), base + y * rs, ok);
+    }
+}
+
+// Stores T columns of a tile buffer back (columns >= ncol skipped).
+template <class C, int ROWS>
+__device__ __forceinline__ void store_cols(float2 *dst, int64_t rs, int l0, int ncol,
+                                           const float2 *buf) {
+    constexpr int T = C::T;
+    for (int it = threadIdx.x; it < ROWS * T; it += C::TH) {
+        const int t = it % T, y = it / T;
+        if (l0 + t < ncol) dst[(int64_t)y * rs + l0 + t] = buf[C::at(t, y)];
+    }
+}
+
+struct PGeom {
+    int64_t nplanes;
+};
+
+// Forward plane transform: real planes (n1, 2L) -> complex planes (n1, L+1).
+// Twiddles in ptw: [exp(-2 pi i m / N1), m < N1 | exp(-2 pi i m / L), m < L |
+// exp(-2 pi i k / 2L), k <= L].
+template <int N1, int L>
+__global__ void __launch_bounds__(PTH, 1) k_plane_r2c(const float *__restrict__ in,
+                                                      float2 *__restrict__ out,
+                                                      const float2 *__restrict__ ptw, PGeom g) {
+    using ZC = XCfg<L, PTH>;
+    using YC = XCfg<N1, PTH>;
+    constexpr int N2 = 2 * L, N2H = L + 1, RPC = N1 / PCL;
+    constexpr int ZT = ZC::T, NB = (RPC + ZT - 1) / ZT;
+    constexpr int YT = YC::T, NTILE = (N2H + YT - 1) / YT;
+    constexpr int ZREG = 2 * ZC::BUF, YREG = 2 * YC::BUF;
+    constexpr int REG = ZREG > YREG ? ZREG : YREG;
+    extern __shared__ __align__(16) float2 smem2[];
+    float2 *twY = smem2 + REG, *twL = twY + N1, *twN = twL + L;
+    for (int m = threadIdx.x; m < N1 + L + N2H; m += PTH) twY[m] = ptw[m];
+
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int64_t cid = blockIdx.x / PCL, ncl = gridDim.x / PCL;
+    const int yb = rank * RPC;
+
+    for (int64_t p = cid; p < g.nplanes; p += ncl) {
+        const float2 *src = reinterpret_cast<const float2 *>(in + p * (int64_t)N1 * N2);
+        float2 *dst = out + p * (int64_t)N1 * N2H;
+        // rows [yb, yb + RPC): half-length FFT, then the real-input split
+        auto issue_rows = [&](int b, float2 *buf) {
+            for (int it = threadIdx.x; it < ZT * L; it += PTH) {
+                const int t = it / L, m = it % L, y = b * ZT + t;
+                const bool ok = y < RPC;
+                cp_async8(buf + ZC::at(t, m), src + (int64_t)(yb + (ok ? y : 0)) * L + m, ok);
+            }
+        };
+        issue_rows(0, smem2);
+        cp_async_commit();
+        for (int b = 0; b < NB; ++b) {
+            float2 *buf = smem2 + (b & 1) * ZC::BUF;
+            cp_async_wait_all();
+            __syncthreads();
+            if (b + 1 < NB) issue_rows(b + 1, smem2 + ((b + 1) & 1) * ZC::BUF);
+            cp_async_commit();
+            fft_cols<ZC, false>(buf, twL);
+            for (int it = threadIdx.x; it < ZT * N2H; it += PTH) {
+                const int t = it / N2H, k = it % N2H, y = b * ZT + t;
+                if (y >= RPC) continue;
+                const float2 zk = buf[ZC::at(t, k == L ? 0 : k)];
+                const float2 zm = buf[ZC::at(t, k == 0 ? 0 : L - k)];
+                const float2 e = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+                const float2 o = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+                const float2 w = twN[k];
+                dst[(int64_t)(yb + y) * N2H + k] =
+                    make_float2(e.x + (w.x * o.x - w.y * o.y), e.y + (w.x * o.y + w.y * o.x));
+            }
+        }
+        cp_async_wait_all();
+        cl.sync();  // every row of the plane is written (and visible)
+        // columns: tiles rank, rank + PCL, ...
+        int tl = rank;
+        if (tl < NTILE) issue_cols<YC, N1>(dst, N2H, tl * YT, N2H, smem2);
+        cp_async_commit();
+        for (int i = 0; tl < NTILE; tl += PCL, ++i) {
+            float2 *buf = smem2 + (i & 1) * YC::BUF;
+            cp_async_wait_all();
+            __syncthreads();
+            if (tl + PCL < NTILE)
+                issue_cols<YC, N1>(dst, N2H, (tl + PCL) * YT, N2H, smem2 + ((i + 1) & 1) * YC::BUF);
+            cp_async_commit();
+            fft_cols<YC, false>(buf, twY);
+            store_cols<YC, N1>(dst, N2H, tl * YT, N2H, buf);
+        }
+        cp_async_wait_all();
+        __syncthreads();  // tile buffers free before the next plane's rows
+    }
+}
+
+// Inverse plane transform: complex planes (n1, L+1) -> real planes (n1, 2L).
+// The complex input is transformed in place along y first (destroyed).
+template <int N1, int L>
+__global__ void __launch_bounds__(PTH, 1) k_plane_c2r(float2 *__restrict__ in,
+                                                      float *__restrict__ out,
+                                                      const float2 *__restrict__ ptw, PGeom g) {
+    using ZC = XCfg<L, PTH>;
+    using YC = XCfg<N1, PTH>;
+    constexpr int N2 = 2 * L, N2H = L + 1, RPC = N1 / PCL;
+    constexpr int ZT = ZC::T, NB = (RPC + ZT - 1) / ZT;
+    constexpr int YT = YC::T, NTILE = (N2H + YT - 1) / YT;
+    constexpr int XRS = N2H + 1;  // raw row stride in shared memory
+    constexpr int ZREG = 2 * ZT * XRS + ZC::BUF, YREG = 2 * YC::BUF;
+    constexpr int REG = ZREG > YREG ? ZREG : YREG;
+    extern __shared__ __align__(16) float2 smem2[];
+    float2 *twY = smem2 + REG, *twL = twY + N1, *twN = twL + L;
+    for (int m = threadIdx.x; m < N1 + L + N2H; m += PTH) twY[m] = ptw[m];
+
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int64_t cid = blockIdx.x / PCL, ncl = gridDim.x / PCL;
+    const int yb = rank * RPC;
+
+    for (int64_t p = cid; p < g.nplanes; p += ncl) {
+        float2 *cpl = in + p * (int64_t)N1 * N2H;
+        float2 *rpl = reinterpret_cast<float2 *>(out + p * (int64_t)N1 * N2);
+        // columns first (inverse along y, in place)
+        int tl = rank;
+        if (tl < NTILE) issue_cols<YC, N1>(cpl, N2H, tl * YT, N2H, smem2);
+        cp_async_commit();
+        for (int i = 0; tl < NTILE; tl += PCL, ++i) {
+            float2 *buf = smem2 + (i & 1) * YC::BUF;
+            cp_async_wait_all();
+            __syncthreads();
+            if (tl + PCL < NTILE)
+                issue_cols<YC, N1>(cpl, N2H, (tl + PCL) * YT, N2H, smem2 + ((i + 1) & 1) * YC::BUF);
+            cp_async_commit();
+            fft_cols<YC, true>(buf, twY);
+            store_cols<YC, N1>(cpl, N2H, tl * YT, N2H, buf);
+        }
+        cp_async_wait_all();
+        cl.sync();  // every column of the plane is transformed (and visible)
+        // rows [yb, yb + RPC): Hermitian rebuild, half-length inverse FFT
+        float2 *F = smem2 + 2 * ZT * XRS;
+        auto issue_rows = [&](int b, float2 *raw) {
+            for (int it = threadIdx.x; it < ZT * N2H; it += PTH) {
+                const int t = it / N2H, k = it % N2H, y = b * ZT + t;
+                const bool ok = y < RPC;
+                cp_async8(raw + t * XRS + k, cpl + (int64_t)(yb + (ok ? y : 0)) * N2H + k, ok);
+            }
+        };
+        issue_rows(0, smem2);
+        cp_async_commit();
+        for (int b = 0; b < NB; ++b) {
+            const float2 *raw = smem2 + (b & 1) * ZT * XRS;
+            cp_async_wait_all();
+            __syncthreads();
+            if (b + 1 < NB) issue_rows(b + 1, smem2 + ((b + 1) & 1) * ZT * XRS);
+            cp_async_commit();
+            for (int it = threadIdx.x; it < ZT * L; it += PTH) {
+                const int t = it / L, k = it % L;
+                float2 xk = raw[t * XRS + k], xm = raw[t * XRS + (L - k)];
+                if (k == 0) {
+                    xk.y = 0.f;
+                    xm.y = 0.f;
+                }
+                const float2 s = make_float2(xk.x + xm.x, xk.y - xm.y);  // X[k] + conj X[L-k]
+                const float2 d = make_float2(xk.x - xm.x, xk.y + xm.y);  // X[k] - conj X[L-k]
+                const float2 w = twN[k];                                  // w_N^k; use conj
+                const float2 dw = make_float2(d.x * w.x + d.y * w.y, d.y * w.x - d.x * w.y);
+                F[ZC::at(t, k)] = make_float2(s.x - dw.y, s.y + dw.x);    // s + i d conj(w)
+            }
+            __syncthreads();
+            fft_cols<ZC, true>(F, twL);
+            for (int it = threadIdx.x; it < ZT * L; it += PTH) {
+                const int t = it / L, m = it % L, y = b * ZT + t;
+                if (y < RPC) rpl[(int64_t)(yb + y) * L + m] = F[ZC::at(t, m)];
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+    }
+}
+
+template <int N1, int L>
+size_t plane_smem(bool inv) {
+    using ZC = XCfg<L, PTH>;
+    using YC = XCfg<N1, PTH>;
+    const int zreg = inv ? 2 * ZC::T * (L + 2) + ZC::BUF : 2 * ZC::BUF;
+    const int yreg = 2 * YC::BUF;
+    const int reg = zreg > yreg ? zreg : yreg;
+    return (size_t)(reg + N1 + L + L + 1) * sizeof(float2);
+}
+
+template <int N1, int L>
+int launch_plane(bool inv, const void *in, void *out, const float2 *ptw, int64_t nplanes,
+                 cudaStream_t st) {
+    const size_t sm = plane_smem<N1, L>(inv);
+    const void *fn = inv ? (const void *)k_plane_c2r<N1, L> : (const void *)k_plane_r2c<N1, L>;
+    PMX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = PCL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(PTH);
+    cfg.dynamicSmemBytes = sm;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(PCL);
+    int ncl = 0;
+    PMX_CUDA(cudaOccupancyMaxActiveClusters(&ncl, fn, &cfg));
+    if (ncl < 1) return fail(PMX_ERR_CUDA, "plane transform cluster does not fit on the GPU");
+    if (ncl > nplanes) ncl = (int)nplanes;
+    cfg.gridDim = dim3(ncl * PCL);
+    PGeom g;
+    g.nplanes = nplanes;
+    if (inv) {
+        PMX_CUDA(cudaLaunchKernelEx(&cfg, k_plane_c2r<N1, L>, (float2 *)in, (float *)out, ptw, g));
+        PMX_LAUNCH_CHECK("k_plane_c2r");
+    } else {
+        PMX_CUDA(cudaLaunchKernelEx(&cfg, k_plane_r2c<N1, L>, (const float *)in, (float2 *)out, ptw, g));
+        PMX_LAUNCH_CHECK("k_plane_r2c");
     }
     return PMX_OK;
 }
@@ -499,6 +876,43 @@ void xpass_twiddles(int64_t n, float2 *host) {
     for (int64_t m = 0; m < n; ++m) {
         double a = -2.0 * kPi * (double)m / (double)n;
         host[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+}
+
+
+bool plane_supported(int64_t n1, int64_t n2) {
+    return n1 == n2 && (n1 == 64 || n1 == 128 || n1 == 256 || n1 == 512 || n1 == 1024);
+}
+
+int plane_fft(bool inv, const void *in, void *out, const float2 *ptw, int64_t nplanes, int64_t n1,
+              int64_t n2, cudaStream_t st) {
+    if (!plane_supported(n1, n2)) return fail(PMX_ERR_SHAPE, "plane transform needs square power-of-two planes 64..1024");
+    if (nplanes < 1) return PMX_OK;
+    switch (n1) {
+        case 64: return launch_plane<64, 32>(inv, in, out, ptw, nplanes, st);
+        case 128: return launch_plane<128, 64>(inv, in, out, ptw, nplanes, st);
+        case 256: return launch_plane<256, 128>(inv, in, out, ptw, nplanes, st);
+        case 512: return launch_plane<512, 256>(inv, in, out, ptw, nplanes, st);
+        default: return launch_plane<1024, 512>(inv, in, out, ptw, nplanes, st);
+    }
+}
+
+// [exp(-2 pi i m / n1), m < n1 | exp(-2 pi i m / L), m < L | exp(-2 pi i k / n2), k <= L],
+// L = n2 / 2; float64 on the host, then float32.
+void plane_twiddles(int64_t n1, int64_t n2, float2 *host) {
+    const int64_t L = n2 / 2;
+    int64_t o = 0;
+    for (int64_t m = 0; m < n1; ++m, ++o) {
+        double a = -2.0 * kPi * (double)m / (double)n1;
+        host[o] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    for (int64_t m = 0; m < L; ++m, ++o) {
+        double a = -2.0 * kPi * (double)m / (double)L;
+        host[o] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    for (int64_t k = 0; k <= L; ++k, ++o) {
+        double a = -2.0 * kPi * (double)k / (double)n2;
+        host[o] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
 }
 

@@ -59,6 +59,25 @@ const char *cufft_name(cufftResult r) {
 
 }  // namespace
 
+namespace pmx {
+namespace slabs {
+constexpr int KMAX = 4;  // most concurrent slab chains
+// One slab-wise 2-D transform: a cuFFT plan (with its own work area) per
+// chain, and the captured graph of the whole slab loop.
+struct SlabXf {
+    cufftHandle plan[KMAX] = {};
+    bool have[KMAX] = {};
+    void *work[KMAX] = {};
+    bool r2c = true;
+    cudaGraphExec_t exec = nullptr;
+    const void *in = nullptr;   // buffers the graph was captured with
+    void *out = nullptr;
+};
+}  // namespace slabs
+}  // namespace pmx
+using pmx::slabs::SlabXf;
+using pmx::slabs::KMAX;
+
 struct pmx_workspace {
     int dev = 0;
     int flags = 0;
@@ -80,8 +99,17 @@ struct pmx_workspace {
     bool win = false;           // warp-window deposits (n2 % 4 == 0)
     int64_t slab = 0;           // x-planes per 2-D cuFFT execution
     float2 *tw = nullptr;       // exp(-2 pi i m / n0)
-    cufftHandle p2r = 0, p2c3 = 0, p2r3 = 0, p2c = 0;  // 2-D r2c, c2r x3, r2c x3, c2r
-    bool have_p2r = false, have_p2c3 = false, have_p2r3 = false, have_p2c = false;
+    // square power-of-two planes: the (y, z) transforms are the cluster
+    // plane kernels of pmx_fft.cu instead of 2-D cuFFT
+    bool plane = false;
+    float2 *ptw = nullptr;      // plane_twiddles(n1, n2)
+    // slab-wise 2-D cuFFT: kinds 0..3 = r2c of the density, c2r of the three
+    // gradient spectra, r2c of the three mesh cotangents, c2r of the adjoint
+    SlabXf sx[4];
+    int nbranch = 1;            // concurrent slab chains (streams)
+    bool graphs = false;        // slab loops captured as CUDA graphs
+    cudaStream_t cap = nullptr, aux[KMAX] = {};
+    cudaEvent_t fork = nullptr, join[KMAX] = {};
     // stage profiler: CUDA events around every stage while enabled
     bool prof_on = false;
     struct Rec {
@@ -848,6 +876,66 @@ int poisson_grid(pmx_workspace *ws) {
     return (int)(blocks < cap ? blocks : cap);
 }
 
+// Issues the slab loop of transform `kind` on stream s0: slab i (S x-planes
+// of one component) runs on chain i % nbranch, each chain on its own stream
+// with its own plan, forked from and joined back into s0.
+int slab_issue(pmx_workspace *ws, int kind, const void *in, void *out, cudaStream_t s0) {
+    SlabXf &x = ws->sx[kind];
+    const int64_t pr = ws->n1 * ws->n2, pc = ws->n1 * ws->n2h, S = ws->slab;
+    const int64_t np = (kind == 1 || kind == 2) ? 3 * ws->n0 : ws->n0;
+    const int K = ws->nbranch;
+    if (K > 1) {
+        PMX_CUDA(cudaEventRecord(ws->fork, s0));
+        for (int k = 1; k < K; ++k) PMX_CUDA(cudaStreamWaitEvent(ws->aux[k], ws->fork, 0));
+    }
+    for (int64_t p = 0, i = 0; p < np; p += S, ++i) {
+        const int k = (int)(i % K);
+        PMX_CUFFT(cufftSetStream(x.plan[k], k ? ws->aux[k] : s0));
+        if (x.r2c)
+            PMX_CUFFT(cufftExecR2C(x.plan[k], (float *)in + p * pr, (cufftComplex *)out + p * pc));
+        else
+            PMX_CUFFT(cufftExecC2R(x.plan[k], (cufftComplex *)in + p * pc, (float *)out + p * pr));
+    }
+    for (int k = 1; k < K; ++k) {
+        PMX_CUDA(cudaEventRecord(ws->join[k], ws->aux[k]));
+        PMX_CUDA(cudaStreamWaitEvent(s0, ws->join[k], 0));
+    }
+    return PMX_OK;
+}
+
+// Runs transform `kind` (in -> out, all planes) on st: directly, or by
+// launching the CUDA graph of its slab loop, captured on first use (and again
+// if the buffers change).
+int slab_run(pmx_workspace *ws, int kind, const void *in, void *out, cudaStream_t st) {
+    if (!ws->graphs) return slab_issue(ws, kind, in, out, st);
+    SlabXf &x = ws->sx[kind];
+    if (x.exec && (x.in != in || x.out != out)) {
+        cudaGraphExecDestroy(x.exec);
+        x.exec = nullptr;
+    }
+    if (!x.exec) {
+        PMX_CUDA(cudaStreamBeginCapture(ws->cap, cudaStreamCaptureModeThreadLocal));
+        int e = slab_issue(ws, kind, in, out, ws->cap);
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(ws->cap, &g);
+        if (e) {
+            if (g) cudaGraphDestroy(g);
+            return e;
+        }
+        if (ce != cudaSuccess) return cuda_status(ce, "slab graph capture");
+        ce = cudaGraphInstantiate(&x.exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            x.exec = nullptr;
+            return cuda_status(ce, "slab graph instantiate");
+        }
+        x.in = in;
+        x.out = out;
+    }
+    PMX_CUDA(cudaGraphLaunch(x.exec, st));
+    return PMX_OK;
+}
+
 // Forward force up to the three acceleration meshes in ws->g.  With kd, the
 // kick/drift of the forward step (or kick_adj/drift_adj of the reverse step
 // when adj) precede the density deposit.
@@ -855,26 +943,29 @@ int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t s
     float s = (float)(1.5 * (double)(float)omega_m);
     float c = (float)((double)s / (double)ws->M);
     if (ws->xfast) {
-        const int64_t pr = ws->n1 * ws->n2, pc = ws->n1 * ws->n2h, S = ws->slab;
         float2 *H = reinterpret_cast<float2 *>(ws->g);  // g is free until the c2r
-        {
+        if (ws->plane) {
+            Stage sg(ws, 2, st, 1);
+            int st2 = plane_fft(false, ws->dens, H, ws->ptw, ws->n0, ws->n1, ws->n2, st);
+            if (st2) return st2;
+        } else {
             Stage sg(ws, 2, st, 0);
-            PMX_CUFFT(cufftSetStream(ws->p2r, st));
-            for (int64_t x = 0; x < ws->n0; x += S)
-                PMX_CUFFT(cufftExecR2C(ws->p2r, ws->dens + x * pr,
-                                       reinterpret_cast<cufftComplex *>(H + x * pc)));
+            int st2 = slab_run(ws, 0, ws->dens, H, st);
+            if (st2) return st2;
         }
         {
             Stage sg(ws, 3, st, 1);
             int st2 = xpass(false, H, ws->ck, ws->ktab, ws->tw, ws->n0, ws->n1, ws->n2h, c, st);
             if (st2) return st2;
         }
-        {
+        if (ws->plane) {
+            Stage sg(ws, 4, st, 1);
+            int st2 = plane_fft(true, ws->ck, ws->g, ws->ptw, 3 * ws->n0, ws->n1, ws->n2, st);
+            if (st2) return st2;
+        } else {
             Stage sg(ws, 4, st, 0);
-            PMX_CUFFT(cufftSetStream(ws->p2c3, st));
-            for (int64_t x = 0; x < ws->n0; x += S)
-                PMX_CUFFT(cufftExecC2R(ws->p2c3, reinterpret_cast<cufftComplex *>(ws->ck + 3 * x * pc),
-                                       ws->g + 3 * x * pr));
+            int st2 = slab_run(ws, 1, ws->ck, ws->g, st);
+            if (st2) return st2;
         }
         return PMX_OK;
     }
@@ -904,26 +995,29 @@ int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
     float s = (float)(1.5 * (double)(float)omega_m);
     float c = (float)((double)s / (double)ws->M);
     if (ws->xfast) {
-        const int64_t pr = ws->n1 * ws->n2, pc = ws->n1 * ws->n2h, S = ws->slab;
         float2 *Sk = reinterpret_cast<float2 *>(ws->g);  // g is dead after k_g3adj
-        {
+        if (ws->plane) {
+            Stage sg(ws, 8, st, 1);
+            int st2 = plane_fft(false, ws->mcot, ws->ck, ws->ptw, 3 * ws->n0, ws->n1, ws->n2, st);
+            if (st2) return st2;
+        } else {
             Stage sg(ws, 8, st, 0);
-            PMX_CUFFT(cufftSetStream(ws->p2r3, st));
-            for (int64_t x = 0; x < ws->n0; x += S)
-                PMX_CUFFT(cufftExecR2C(ws->p2r3, ws->mcot + 3 * x * pr,
-                                       reinterpret_cast<cufftComplex *>(ws->ck + 3 * x * pc)));
+            int st2 = slab_run(ws, 2, ws->mcot, ws->ck, st);
+            if (st2) return st2;
         }
         {
             Stage sg(ws, 9, st, 1);
             int st2 = xpass(true, ws->ck, Sk, ws->ktab, ws->tw, ws->n0, ws->n1, ws->n2h, c, st);
             if (st2) return st2;
         }
-        {
+        if (ws->plane) {
+            Stage sg(ws, 10, st, 1);
+            int st2 = plane_fft(true, Sk, ws->dens, ws->ptw, ws->n0, ws->n1, ws->n2, st);
+            if (st2) return st2;
+        } else {
             Stage sg(ws, 10, st, 0);
-            PMX_CUFFT(cufftSetStream(ws->p2c, st));
-            for (int64_t x = 0; x < ws->n0; x += S)
-                PMX_CUFFT(cufftExecC2R(ws->p2c, reinterpret_cast<cufftComplex *>(Sk + x * pc),
-                                       ws->dens + x * pr));
+            int st2 = slab_run(ws, 3, Sk, ws->dens, st);
+            if (st2) return st2;
         }
         return PMX_OK;
     }
@@ -973,21 +1067,17 @@ int make_plan2d(cufftHandle *plan, int64_t n1, int64_t n2, cufftType type, int64
     return PMX_OK;
 }
 
-// x-planes per 2-D cuFFT execution: PMX_SLAB if set, else the largest power
-// of two dividing n0 whose three-component slab (real + complex planes)
-// stays within 64 MB, so each slab's intermediate stays in L2.
-int64_t choose_slab(int64_t n0, int64_t n1, int64_t n2) {
+// x-planes per 2-D cuFFT execution: PMX_SLAB if set, else 8, so that the
+// intermediate of every concurrent execution stays in L2 (the slab loops run
+// as captured CUDA graphs, which removes the per-call launch cost).
+int64_t choose_slab(int64_t n0) {
     const char *env = std::getenv("PMX_SLAB");
     int64_t S = 0;
     if (env) S = std::atoll(env);
-    if (S <= 0) {
-        double plane = (double)n1 * n2 * 4 + (double)n1 * (n2 / 2 + 1) * 8;
-        S = 1;
-        while (S * 2 <= n0 && 3.0 * (S * 2) * plane <= 64.0 * (1 << 20)) S *= 2;
-    }
+    if (S <= 0) S = 8;
+    if (S > n0) S = n0;
     while (S > 1 && n0 % S) S /= 2;
     if (S < 1) S = 1;
-    if (S > n0) S = n0;
     return S;
 }
 
@@ -997,11 +1087,21 @@ void ws_free(pmx_workspace *ws) {
     if (ws->have_c2r3) cufftDestroy(ws->c2r3);
     if (ws->have_r2c3) cufftDestroy(ws->r2c3);
     if (ws->have_c2r1) cufftDestroy(ws->c2r1);
-    if (ws->have_p2r) cufftDestroy(ws->p2r);
-    if (ws->have_p2c3) cufftDestroy(ws->p2c3);
-    if (ws->have_p2r3) cufftDestroy(ws->p2r3);
-    if (ws->have_p2c) cufftDestroy(ws->p2c);
+    for (auto &x : ws->sx) {
+        if (x.exec) cudaGraphExecDestroy(x.exec);
+        for (int k = 0; k < KMAX; ++k) {
+            if (x.have[k]) cufftDestroy(x.plan[k]);
+            cudaFree(x.work[k]);
+        }
+    }
+    for (int k = 0; k < KMAX; ++k) {
+        if (ws->aux[k]) cudaStreamDestroy(ws->aux[k]);
+        if (ws->join[k]) cudaEventDestroy(ws->join[k]);
+    }
+    if (ws->cap) cudaStreamDestroy(ws->cap);
+    if (ws->fork) cudaEventDestroy(ws->fork);
     cudaFree(ws->tw);
+    cudaFree(ws->ptw);
     cudaFree(ws->dens);
     cudaFree(ws->ck);
     cudaFree(ws->g);
@@ -1086,7 +1186,8 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
         return st;
     }
     const char *wenv = std::getenv("PMX_WIN");
-    ws->win = (ws->n2 % 4 == 0) && !(flags & PMX_WS_NO_WINDOW) && !(wenv && wenv[0] == '0');
+    ws->win = (ws->n2 % 4 == 0) && ((flags & PMX_WS_WINDOW) || (wenv && wenv[0] == '1')) &&
+              !(wenv && wenv[0] == '0');
     if (ws->win) {
         cudaError_t e = cudaFuncSetAttribute(k_g3adj, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)WIN3_SMEM);
@@ -1100,18 +1201,56 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
     size_t wk[4] = {0, 0, 0, 0};
     cufftHandle *ph[4];
     bool *hv[4];
+    const char *penv = std::getenv("PMX_PLANE");
+    ws->plane = ws->xfast && plane_supported(ws->n1, ws->n2) &&
+                ((flags & PMX_WS_PLANE) || (penv && penv[0] == '1')) && !(penv && penv[0] == '0');
+    if (ws->plane) {
+        const int64_t np = 2 * ws->n1 + 1;
+        std::vector<float2> ptw(np);
+        plane_twiddles(ws->n1, ws->n2, ptw.data());
+        if ((st = alloc((void **)&ws->ptw, np * sizeof(float2)))) { ws_free(ws); return st; }
+        if (cudaMemcpy(ws->ptw, ptw.data(), np * sizeof(float2), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+            ws_free(ws);
+            return fail(PMX_ERR_CUDA, "plane twiddle upload failed");
+        }
+    }
     if (ws->xfast) {
-        ws->slab = choose_slab(ws->n0, ws->n1, ws->n2);
+        ws->slab = choose_slab(ws->n0);
         const int64_t S = ws->slab;
-        if ((st = make_plan2d(&ws->p2r, ws->n1, ws->n2, CUFFT_R2C, S, &wk[0]))) { ws_free(ws); return st; }
-        ws->have_p2r = true;
-        if ((st = make_plan2d(&ws->p2c3, ws->n1, ws->n2, CUFFT_C2R, 3 * S, &wk[1]))) { ws_free(ws); return st; }
-        ws->have_p2c3 = true;
-        if (flags & PMX_WS_ADJOINT) {
-            if ((st = make_plan2d(&ws->p2r3, ws->n1, ws->n2, CUFFT_R2C, 3 * S, &wk[2]))) { ws_free(ws); return st; }
-            ws->have_p2r3 = true;
-            if ((st = make_plan2d(&ws->p2c, ws->n1, ws->n2, CUFFT_C2R, S, &wk[3]))) { ws_free(ws); return st; }
-            ws->have_p2c = true;
+        if (!ws->plane) {
+            const char *kenv = std::getenv("PMX_SLAB_CHAINS");
+            const char *genv = std::getenv("PMX_SLAB_GRAPH");
+            int K = kenv ? std::atoi(kenv) : 2;
+            ws->nbranch = K < 1 ? 1 : (K > KMAX ? KMAX : K);
+            ws->graphs = !(genv && genv[0] == '0');
+            auto mk_stream = [&](cudaStream_t *sp) -> int {
+                cudaError_t e = cudaStreamCreateWithFlags(sp, cudaStreamNonBlocking);
+                return e == cudaSuccess ? PMX_OK : cuda_status(e, "cudaStreamCreate");
+            };
+            auto mk_event = [&](cudaEvent_t *ep) -> int {
+                cudaError_t e = cudaEventCreateWithFlags(ep, cudaEventDisableTiming);
+                return e == cudaSuccess ? PMX_OK : cuda_status(e, "cudaEventCreate");
+            };
+            if ((st = mk_stream(&ws->cap)) || (st = mk_event(&ws->fork))) { ws_free(ws); return st; }
+            for (int k = 1; k < ws->nbranch; ++k)
+                if ((st = mk_stream(&ws->aux[k])) || (st = mk_event(&ws->join[k]))) { ws_free(ws); return st; }
+            const int nkind = (flags & PMX_WS_ADJOINT) ? 4 : 2;
+            for (int kind = 0; kind < nkind; ++kind) {
+                SlabXf &x = ws->sx[kind];
+                x.r2c = kind == 0 || kind == 2;
+                for (int k = 0; k < ws->nbranch; ++k) {
+                    size_t w = 0;
+                    if ((st = make_plan2d(&x.plan[k], ws->n1, ws->n2, x.r2c ? CUFFT_R2C : CUFFT_C2R, S, &w))) { ws_free(ws); return st; }
+                    x.have[k] = true;
+                    if (w > 0 && (st = alloc(&x.work[k], w))) { ws_free(ws); return st; }
+                    cufftResult r = cufftSetWorkArea(x.plan[k], x.work[k]);
+                    if (r != CUFFT_SUCCESS) {
+                        ws_free(ws);
+                        return fail(PMX_ERR_CUFFT, std::string("cufftSetWorkArea: ") + cufft_name(r));
+                    }
+                }
+            }
         }
         std::vector<float2> tw(ws->n0);
         xpass_twiddles(ws->n0, tw.data());
@@ -1121,8 +1260,10 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
             ws_free(ws);
             return fail(PMX_ERR_CUDA, "twiddle upload failed");
         }
-        ph[0] = &ws->p2r; ph[1] = &ws->p2c3; ph[2] = &ws->p2r3; ph[3] = &ws->p2c;
-        hv[0] = &ws->have_p2r; hv[1] = &ws->have_p2c3; hv[2] = &ws->have_p2r3; hv[3] = &ws->have_p2c;
+        for (int i = 0; i < 4; ++i) {
+            ph[i] = nullptr;
+            hv[i] = nullptr;
+        }
     } else {
         int64_t shp[3] = {ws->n0, ws->n1, ws->n2};
         if ((st = make_plan(&ws->r2c1, shp, CUFFT_R2C, 1, &wk[0]))) { ws_free(ws); return st; }
@@ -1144,7 +1285,7 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
     if (wmax > 0 && (st = alloc(&ws->fft_work, wmax))) { ws_free(ws); return st; }
     ws->fft_work_bytes = wmax;
     for (int i = 0; i < 4; ++i) {
-        if (!*hv[i]) continue;
+        if (!hv[i] || !*hv[i]) continue;
         cufftResult r = cufftSetWorkArea(*ph[i], ws->fft_work);
         if (r != CUFFT_SUCCESS) {
             ws_free(ws);

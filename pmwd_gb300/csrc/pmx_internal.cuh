@@ -81,6 +81,15 @@ int xpass(bool adj, const float2 *in, float2 *out, const float *kt, const float2
           int64_t n1, int64_t n2h, float c, cudaStream_t st);
 void xpass_twiddles(int64_t n, float2 *host);
 
+// 2-D (y, z) transforms of consecutive planes (pmx_fft.cu): forward real
+// (n1, n2) -> complex (n1, n2/2+1), inverse complex -> real (input
+// destroyed); one thread-block cluster per plane.  ptw holds
+// plane_twiddles(n1, n2) (2 n1 + 1 entries for square planes).
+bool plane_supported(int64_t n1, int64_t n2);
+int plane_fft(bool inv, const void *in, void *out, const float2 *ptw, int64_t nplanes, int64_t n1,
+              int64_t n2, cudaStream_t st);
+void plane_twiddles(int64_t n1, int64_t n2, float2 *host);
+
 __device__ __forceinline__ int pymod(int x, int m) {
     int r = x % m;
     return r < 0 ? r + m : r;

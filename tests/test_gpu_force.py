@@ -53,12 +53,14 @@ XPASS_CASES = [((32, 32, 32), 2, 1.0), ((32, 16, 24), 4, 2.0), ((64, 64, 64), 1,
                ((128, 64, 32), 1, 1.0), ((128, 128, 128), 2, 2.0)]
 
 
-def _force_both_paths(cuda, gconf, pmid, disp, cot=None):
-    """pmx_force / pmx_force_vjp on a fused-x-pass workspace and on a 3-D
-    cuFFT workspace."""
+def _force_both_paths(cuda, gconf, pmid, disp, cot=None,
+                      variants=({}, {'cufft3d': True})):
+    """pmx_force / pmx_force_vjp on workspaces built with each set of
+    keyword flags in `variants` (default: the fused x-pass path and the 3-D
+    cuFFT path)."""
     out = []
-    for cufft3d in (False, True):
-        ws = _lib.Workspace(gconf.mesh_shape, adjoint=True, cufft3d=cufft3d)
+    for kw in variants:
+        ws = _lib.Workspace(gconf.mesh_shape, adjoint=True, **kw)
         spec = _lib.make_spec(3, gconf.mesh_shape, gconf.mesh_shape, gconf.cell_size)
         n = len(pmid)
         P, D = T(pmid, cuda), T(disp, cuda)
@@ -79,8 +81,8 @@ def _force_both_paths(cuda, gconf, pmid, disp, cot=None):
 
 @pytest.mark.parametrize('ptcl, mesh, spacing', XPASS_CASES)
 def test_fused_xpass_force_matches_oracle(cuda, ptcl, mesh, spacing):
-    """Power-of-two n0 (64..1024) takes the slab 2-D cuFFT + fused x-pass
-    path; it must match the oracle and the 3-D cuFFT path."""
+    """Power-of-two n0 (64..1024) takes the fused x-pass path (slab-wise
+    2-D cuFFT planes); it must match the oracle and the 3-D cuFFT path."""
     oconf, gconf, pmid, disp, vel = make(ptcl, mesh, spacing, 1.5 * spacing)
     acc_o = pm.gravity(pmid, disp, 0.3, oconf)
     fast, ref3d = _force_both_paths(cuda, gconf, pmid, disp)
@@ -101,6 +103,29 @@ def test_fused_xpass_force_vjp_matches_oracle(cuda, ptcl, mesh, spacing):
         assert rel_l2(a, acc_o) < RTOL_ACC
         assert rel_l2(dc, dc_o) < 1e-4
         assert abs(om / om_o - 1) < 1e-4
+
+
+PLANE_CASES = [((16, 64, 64), 4, 1.0), ((16, 128, 128), 4, 1.0), ((16, 256, 256), 4, 1.0)]
+
+
+@pytest.mark.parametrize('ptcl, mesh, spacing', PLANE_CASES)
+def test_plane_transforms_match_cufft_and_oracle(cuda, ptcl, mesh, spacing):
+    """Square power-of-two (y, z) planes of 256^2, 512^2 and 1024^2 through
+    the cluster plane kernels and through slab-wise 2-D cuFFT: force and
+    force VJP must match each other, the 3-D cuFFT path and the oracle."""
+    oconf, gconf, pmid, disp, vel = make(ptcl, mesh, spacing, 1.5 * spacing)
+    variants = ({'plane': True}, {}, {'cufft3d': True})
+    acc_o = pm.gravity(pmid, disp, 0.3, oconf)
+    accs = _force_both_paths(cuda, gconf, pmid, disp, variants=variants)
+    for a in accs:
+        assert rel_l2(a, acc_o) < RTOL_ACC
+    assert rel_l2(accs[0], accs[1]) < RTOL_ACC
+    cot = np.random.default_rng(5).normal(size=disp.shape).astype(np.float32)
+    res = _force_both_paths(cuda, gconf, pmid, disp, cot, variants=variants)
+    for a, dc, om in res[1:]:
+        assert rel_l2(res[0][0], a) < RTOL_ACC
+        assert rel_l2(res[0][1], dc) < 1e-4
+        assert abs(res[0][2] / om - 1) < 1e-4
 
 
 @pytest.mark.parametrize('ptcl, mesh', [((16, 16, 16), 2), ((10, 12, 14), 1)])

@@ -14,8 +14,8 @@ pytestmark = pytest.mark.gpu
 
 
 def rel_l2(a, b):
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
+    a = np.asarray(a, np.complex128)   # real or complex (Fourier modes)
+    b = np.asarray(b, np.complex128)
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
