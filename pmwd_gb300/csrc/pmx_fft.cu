@@ -277,10 +277,22 @@ __device__ __forceinline__ void inv_step2_store(float2 (&v)[C::R2], float2 *buf,
     }
 }
 
+// Column tiles of a ky row j start at l0 = s_j + (k - 1) T, k < ncol_tiles,
+// with s_j = (-j n2h) mod 4: every tile but the first and last of a row then
+// covers whole 32-byte sectors of every x-plane (the plane size n1 n2h is a
+// multiple of 4 then).  HBM3e has no byte-masked writes, so partial-sector
+// stores would cost read-modify-writes.  Columns outside [0, n2h) are idle.
 struct XGeom {
     int64_t n1, n2h;
-    int64_t ncol_tiles;   // ceil(n2h / T)
+    int64_t ncol_tiles;   // ceil(n2h / T) + 1
+    int align;            // 1: shift rows as above (n1 n2h % 4 == 0)
     float c;              // 1.5 Omega_m / N
+    __device__ __forceinline__ int64_t row(int64_t tile) const { return tile / ncol_tiles; }
+    __device__ __forceinline__ int64_t col0(int64_t tile, int T) const {
+        const int64_t j = tile / ncol_tiles, k = tile % ncol_tiles;
+        const int64_t sj = align ? (4 - (j * n2h) % 4) % 4 : 0;
+        return sj + (k - 1) * T;
+    }
 };
 
 // Starts the asynchronous load of the column tile (fixed ky row j, kz in
@@ -292,7 +304,7 @@ __device__ __forceinline__ void issue_tile(const float2 *__restrict__ src, int n
     constexpr int T = C::T, XS = C::TH / C::T;
     const int t = threadIdx.x % T, x0 = threadIdx.x / T;
     const int64_t l = l0 + t;
-    const bool ok = l < g.n2h;
+    const bool ok = l >= 0 && l < g.n2h;
     const float2 *base = src + ((int64_t)comp * g.n1 + j) * g.n2h + (ok ? l : 0);
     const int64_t xs = (int64_t)ncomp * g.n1 * g.n2h;
 #pragma unroll 8
@@ -330,20 +342,18 @@ __global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__
 
     const int64_t ntiles = g.n1 * g.ncol_tiles;
     int64_t tile = blockIdx.x;
-    if (tile < ntiles)
-        issue_tile<C>(H, 1, 0, tile / g.ncol_tiles, (tile % g.ncol_tiles) * T, g, A0);
+    if (tile < ntiles) issue_tile<C>(H, 1, 0, g.row(tile), g.col0(tile, T), g, A0);
     cp_async_commit();
     for (int cur = 0; tile < ntiles; tile += gridDim.x, cur ^= 1) {
         float2 *A = cur ? A1 : A0;
-        const int64_t j = tile / g.ncol_tiles;
-        const int64_t l0 = (tile % g.ncol_tiles) * T;
+        const int64_t j = g.row(tile);
+        const int64_t l0 = g.col0(tile, T);
         cp_async_wait_all();
         // this tile is in A; the previous tile's store phase (reads of the
         // other A buffer and of B) is over; the tables are filled
         __syncthreads();
         const int64_t nxt = tile + gridDim.x;
-        if (nxt < ntiles)
-            issue_tile<C>(H, 1, 0, nxt / g.ncol_tiles, (nxt % g.ncol_tiles) * T, g, cur ? A0 : A1);
+        if (nxt < ntiles) issue_tile<C>(H, 1, 0, g.row(nxt), g.col0(nxt, T), g, cur ? A0 : A1);
         cp_async_commit();
         fwd_step1<C>(A, tw);
         __syncthreads();
@@ -354,7 +364,7 @@ __global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__
         for (int it = threadIdx.x; it < T * R1; it += XTF) {
             const int t = it / R1, k1 = it % R1;
             const int64_t l = l0 + t;
-            const float kzl = l < g.n2h ? __ldg(kz + l) : 0.f;
+            const float kzl = l >= 0 && l < g.n2h ? __ldg(kz + l) : 0.f;
             const float kz2 = __fmul_rn(kzl, kzl);
             float2 v[R2];
 #pragma unroll
@@ -384,7 +394,7 @@ __global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__
             constexpr int XS = XTF / T;
             const int t = threadIdx.x % T;
             const int64_t l = l0 + t;
-            if (l < g.n2h) {
+            if (l >= 0 && l < g.n2h) {
                 const float mzl = __ldg(mz + l);
                 const int64_t cs = g.n1 * g.n2h, xs = 3 * cs;
                 float2 *o = G + j * g.n2h + l;
@@ -402,36 +412,12 @@ __global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__
     cp_async_wait_all();
 }
 
-// Loads B = i ky C_1 + i kz C_2 of a column tile (components 1, 2 of the
-// (x, 3, n1, n2h) array) synchronously, in register batches.
-template <class C>
-__device__ __forceinline__ void load_comb(const float2 *__restrict__ Cin, int64_t j, int64_t l0,
-                                          float myj, const float *__restrict__ mz,
-                                          const XGeom &g, float2 *buf) {
-    constexpr int T = C::T, XS = C::TH / C::T, PER = C::PER, CH = PER < 8 ? PER : 8;
-    const int t = threadIdx.x % T, x0 = threadIdx.x / T;
-    const int64_t l = l0 + t;
-    const bool ok = l < g.n2h;
-    const float mzl = ok ? __ldg(mz + l) : 0.f;
-    const int64_t cs = g.n1 * g.n2h, xs = 3 * cs;
-    const float2 *base = Cin + j * g.n2h + (ok ? l : 0);
-#pragma unroll
-    for (int b = 0; b < PER; b += CH) {
-        float2 c1[CH], c2[CH];
-#pragma unroll
-        for (int r = 0; r < CH; ++r) {
-            const int x = x0 + (b + r) * XS;
-            c1[r] = ok ? __ldg(base + x * xs + cs) : make_float2(0.f, 0.f);
-            c2[r] = ok ? __ldg(base + x * xs + 2 * cs) : make_float2(0.f, 0.f);
-        }
-#pragma unroll
-        for (int r = 0; r < CH; ++r)  // i k (a + i b) = (-k b, k a)
-            buf[C::at(t, x0 + (b + r) * XS)] =
-                make_float2(-__fadd_rn(__fmul_rn(myj, c1[r].y), __fmul_rn(mzl, c2[r].y)),
-                            __fadd_rn(__fmul_rn(myj, c1[r].x), __fmul_rn(mzl, c2[r].x)));
-    }
-}
-
+// Adjoint x pass.  The three input components of a tile rotate through three
+// buffers: while tile i is transformed, the copies of tile i+1 are issued as
+// soon as a buffer frees up (C_0 and C_1 after the fused step, C_2 after the
+// store phase), and tile i+1 waits for C_2 only after the step 1 of C_0 and
+// C_1.  B = i ky C_1 + i kz C_2 is formed after step 1 (the x transform is
+// linear and ky, kz are constant along x).
 template <int N>
 __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__ Cin,
                                                       float2 *__restrict__ S,
@@ -441,7 +427,8 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
     using C = XCfg<N, XTA>;
     constexpr int T = C::T, R1 = C::R1, R2 = C::R2;
     extern __shared__ __align__(16) float2 smem2[];
-    float2 *A0 = smem2, *A1 = smem2 + C::BUF, *B = smem2 + 2 * C::BUF;
+    // buffers of C_0, C_1, C_2 of the current tile (rotated per tile)
+    float2 *A = smem2, *B = smem2 + C::BUF, *P = smem2 + 2 * C::BUF;
     float2 *tw = smem2 + 3 * C::BUF;
     float *kxs = reinterpret_cast<float *>(tw + N), *mxs = kxs + N;
 
@@ -456,39 +443,45 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
 
     const int64_t ntiles = g.n1 * g.ncol_tiles;
     int64_t tile = blockIdx.x;
-    if (tile < ntiles)
-        issue_tile<C>(Cin, 3, 0, tile / g.ncol_tiles, (tile % g.ncol_tiles) * T, g, A0);
-    cp_async_commit();
-    for (int cur = 0; tile < ntiles; tile += gridDim.x, cur ^= 1) {
-        float2 *A = cur ? A1 : A0;
-        const int64_t j = tile / g.ncol_tiles;
-        const int64_t l0 = (tile % g.ncol_tiles) * T;
-        // the previous tile's store phase (reads of the other A buffer) is over
-        __syncthreads();
-        const int64_t nxt = tile + gridDim.x;
-        if (nxt < ntiles)
-            issue_tile<C>(Cin, 3, 0, nxt / g.ncol_tiles, (nxt % g.ncol_tiles) * T, g, cur ? A0 : A1);
+    if (tile < ntiles) {
+        const int64_t j = g.row(tile), l0 = g.col0(tile, T);
+        issue_tile<C>(Cin, 3, 0, j, l0, g, A);
+        issue_tile<C>(Cin, 3, 1, j, l0, g, B);
         cp_async_commit();
-        const float myj = __ldg(my + j);
-        load_comb<C>(Cin, j, l0, myj, mz, g, B);
-        cp_async_wait_group1();  // this tile's C_0 (the next tile's may stay in flight)
+        issue_tile<C>(Cin, 3, 2, j, l0, g, P);
+    }
+    cp_async_commit();
+    for (; tile < ntiles; tile += gridDim.x) {
+        const int64_t j = g.row(tile);
+        const int64_t l0 = g.col0(tile, T);
+        const int64_t nxt = tile + gridDim.x;
+        cp_async_wait_group1();  // C_0, C_1 of this tile
         __syncthreads();
         fwd_step1<C>(A, tw);
         fwd_step1<C>(B, tw);
+        cp_async_wait_all();     // C_2
         __syncthreads();
-        const float kyj = __ldg(ky + j);
+        fwd_step1<C>(P, tw);
+        __syncthreads();
+        const float kyj = __ldg(ky + j), myj = __ldg(my + j);
         const float ky2 = __fmul_rn(kyj, kyj);
         for (int it = threadIdx.x; it < T * R1; it += XTA) {
             const int t = it / R1, k1 = it % R1;
             const int64_t l = l0 + t;
-            const float kzl = l < g.n2h ? __ldg(kz + l) : 0.f;
+            const bool okl = l >= 0 && l < g.n2h;
+            const float kzl = okl ? __ldg(kz + l) : 0.f, mzl = okl ? __ldg(mz + l) : 0.f;
             const float kz2 = __fmul_rn(kzl, kzl);
+            const int q0 = t * C::CS + k1 * (R2 + 1);
             float2 v[R2], w[R2];
 #pragma unroll
-            for (int b = 0; b < R2; ++b) v[b] = A[t * C::CS + k1 * (R2 + 1) + b];
+            for (int b = 0; b < R2; ++b) v[b] = A[q0 + b];
             dft2<R2, false>(v);
 #pragma unroll
-            for (int b = 0; b < R2; ++b) w[b] = B[t * C::CS + k1 * (R2 + 1) + b];
+            for (int b = 0; b < R2; ++b) {  // i ky C_1 + i kz C_2; i k (a + i b) = (-k b, k a)
+                const float2 c1 = B[q0 + b], c2 = P[q0 + b];
+                w[b] = make_float2(-__fadd_rn(__fmul_rn(myj, c1.y), __fmul_rn(mzl, c2.y)),
+                                   __fadd_rn(__fmul_rn(myj, c1.x), __fmul_rn(mzl, c2.x)));
+            }
             dft2<R2, false>(w);
 #pragma unroll
             for (int k = 0; k < R2; ++k) {
@@ -502,19 +495,30 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
             }
             inv_step2_store<C>(v, A, t, k1, tw);
         }
-        __syncthreads();
+        __syncthreads();  // B and P are free: next tile's C_0 into P, C_1 into B
+        if (nxt < ntiles) {
+            issue_tile<C>(Cin, 3, 0, g.row(nxt), g.col0(nxt, T), g, P);
+            issue_tile<C>(Cin, 3, 1, g.row(nxt), g.col0(nxt, T), g, B);
+        }
+        cp_async_commit();
         inv_step1<C>(A);
         __syncthreads();
         {
             constexpr int XS = XTA / T;
             const int t = threadIdx.x % T;
             const int64_t l = l0 + t;
-            if (l < g.n2h) {
+            if (l >= 0 && l < g.n2h) {
                 float2 *o = S + j * g.n2h + l;
                 const int64_t xs = g.n1 * g.n2h;
                 for (int x = threadIdx.x / T; x < N; x += XS) o[x * xs] = A[C::at(t, x)];
             }
         }
+        __syncthreads();  // A is free: next tile's C_2
+        if (nxt < ntiles) issue_tile<C>(Cin, 3, 2, g.row(nxt), g.col0(nxt, T), g, A);
+        cp_async_commit();
+        float2 *const A0 = A;  // next tile: C_0 in P, C_1 in B, C_2 in A
+        A = P;
+        P = A0;
     }
     cp_async_wait_all();
 }
@@ -538,7 +542,8 @@ int launch_xpass(bool adj, const float2 *in, float2 *out, const float *kt, const
     const void *fn = adj ? (const void *)k_xpass_adj<N> : (const void *)k_xpass_fwd<N>;
     const int threads = adj ? XTA : XTF;
     const int T = adj ? XCfg<N, XTA>::T : XCfg<N, XTF>::T;
-    g.ncol_tiles = (n2h + T - 1) / T;
+    g.ncol_tiles = (n2h + T - 1) / T + 1;
+    g.align = (n1 * n2h) % 4 == 0;
     PMX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     int per_sm = 0;
     PMX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, sm));
