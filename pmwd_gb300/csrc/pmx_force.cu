@@ -299,6 +299,9 @@ struct Hot {
     float *dcomp, *vcomp;
     // deposit through per-warp shared-memory windows (needs n2 % 4 == 0)
     bool win;
+    // n2 % 4 == 0: every mesh row starts on 16 bytes, so z-neighbour pairs
+    // inside one aligned group of four floats take one vector reduction
+    bool vec;
 };
 
 __device__ __forceinline__ void hot_axis(const Hot &h, int a, int pm, float d, Axis &ax) {
@@ -361,10 +364,36 @@ __device__ __forceinline__ void hot_enmesh(const Hot &h, const int16_t *pmid, in
     hot_axis(h, 2, pmid[3 * q + 2], d.z, ax[2]);
 }
 
+// Adds a at z index i0 and b at z index i1 (a particle's two z neighbours)
+// of one mesh row: one 16-byte red.global.add.v4.f32 (the other two lanes
+// add zero) when both cells lie in the same aligned group of four floats,
+// else two scalar atomics.  3 of 4 lower-neighbour positions qualify.
+__device__ __forceinline__ void zpair_add(float *row, int i0, int i1, float a, float b, bool vec) {
+    const int r = i0 & 3;
+    if (vec && i1 == i0 + 1 && r != 3) {
+        const float4 v = make_float4(r == 0 ? a : 0.f, r == 0 ? b : (r == 1 ? a : 0.f),
+                                     r == 1 ? b : (r == 2 ? a : 0.f), r == 2 ? b : 0.f);
+        atomicAdd(reinterpret_cast<float4 *>(row + (i0 - r)), v);
+    } else {
+        atomicAdd(row + i0, a);
+        atomicAdd(row + i1, b);
+    }
+}
+
+// Offset of the (x, y) mesh row of neighbour pair p (bit 0: x, bit 1: y).
+__device__ __forceinline__ int64_t hot_row(const Hot &h, const Axis ax[3], int p) {
+    return (int64_t)ax[0].i[p & 1] * h.stride[0] + (int64_t)ax[1].i[(p >> 1) & 1] * h.stride[1];
+}
+
+// CIC deposit of val * frac_k, frac_k = (w_x w_y) w_z as frac_of.
 __device__ __forceinline__ void hot_deposit(const Hot &h, const Axis ax[3], float *dens) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
-        atomicAdd(dens + hot_cell(h, ax, k), __fmul_rn(h.val, frac_of(ax, k)));
+    for (int p = 0; p < 4; ++p) {
+        const float fxy = __fmul_rn(ax[0].w[p & 1], ax[1].w[(p >> 1) & 1]);
+        zpair_add(dens + hot_row(h, ax, p), ax[2].i[0], ax[2].i[1],
+                  __fmul_rn(h.val, __fmul_rn(fxy, ax[2].w[0])),
+                  __fmul_rn(h.val, __fmul_rn(fxy, ax[2].w[1])), h.vec);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -639,10 +668,19 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
                 c0 = __fadd_rn(c0, __fmul_rn(t, fg[0]));
                 c1 = __fadd_rn(c1, __fmul_rn(t, fg[1]));
                 c2 = __fadd_rn(c2, __fmul_rn(t, fg[2]));
-                if (!h.win) {
-                    atomicAdd(mcot + gc, __fmul_rn(vc.x, f));
-                    atomicAdd(mcot + gc + h.gjs, __fmul_rn(vc.y, f));
-                    atomicAdd(mcot + gc + 2 * h.gjs, __fmul_rn(vc.z, f));
+            }
+            if (!h.win) {
+                // gather-VJP mesh term mcot_j[k] += vc_j frac_k
+#pragma unroll
+                for (int p = 0; p < 4; ++p) {
+                    const float fxy = __fmul_rn(ax[0].w[p & 1], ax[1].w[(p >> 1) & 1]);
+                    const float fa = __fmul_rn(fxy, ax[2].w[0]), fb = __fmul_rn(fxy, ax[2].w[1]);
+                    float *row = mcot + hot_row(h, ax, p) + (int64_t)ax[0].i[p & 1] * h.gxs;
+                    const int i0 = ax[2].i[0], i1 = ax[2].i[1];
+                    zpair_add(row, i0, i1, __fmul_rn(vc.x, fa), __fmul_rn(vc.x, fb), h.vec);
+                    zpair_add(row + h.gjs, i0, i1, __fmul_rn(vc.y, fa), __fmul_rn(vc.y, fb), h.vec);
+                    zpair_add(row + 2 * h.gjs, i0, i1, __fmul_rn(vc.z, fa), __fmul_rn(vc.z, fb),
+                              h.vec);
                 }
             }
             float3 a = make_float3(a0, a1, a2);
@@ -846,6 +884,8 @@ int check_hot(pmx_workspace *ws, const pmx_enmesh_spec *spec, const void *pmid, 
     h->dcomp = nullptr;
     h->vcomp = nullptr;
     h->win = ws->win;
+    const char *venv = std::getenv("PMX_VEC");
+    h->vec = ws->n2 % 4 == 0 && !(venv && venv[0] == '0');
     if (ws->xfast) {
         h->gxs = 2 * ws->n1 * ws->n2;
         h->gjs = ws->n1 * ws->n2;
