@@ -227,6 +227,20 @@ def cpu_step_pair_rate(side, mesh, spacing, nbody_steps, reps=1):
     return n, times
 
 
+DATA = 'synthetic: seeded white noise -> E&H linear power -> 2LPT at a=1/64'
+
+
+def workload_config(args, world):
+    """The workload both arms report (the GPU arm runs it whole, the CPU
+    reference arm samples it)."""
+    side = args.ptcl
+    mside = int(round(side * args.mesh))
+    return {'workload': f'{side}^3 ptcl / {mside}^3 mesh, box {side * args.spacing:g} Mpc/h, '
+                        f'1 fwd + 1 adjoint leapfrog step of a {args.nbody_steps}-step run',
+            'ptcl': side ** 3, 'mesh_cells': mside ** 3, 'parallelism': f'replicas x{world}',
+            'l2': 'inputs larger than L2 (mesh 4.3 GB per array)'}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -243,9 +257,8 @@ def run_reference(args, rank):
     line = {'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT,
             'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': 1e3 * sum(timed) / len(timed), 'higher_is_better': True,
-            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-            'config': {'workload': f'{args.ptcl}^3 ptcl / {int(round(args.ptcl * args.mesh))}^3 '
-                                   f'mesh fwd+adjoint step (sampled at {side}^3)'},
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': DATA,
+            'config': workload_config(args, args.gpus),
             'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': cores, 'kind': 'port',
                              'sample': sample},
             'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
@@ -423,12 +436,8 @@ def run_pmx(args, rank, world, local_rank):
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms_step, 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-        'data': 'synthetic: seeded white noise -> E&H linear power -> 2LPT at a=1/64',
-        'config': {'workload': f'{side}^3 ptcl / {conf.mesh_shape[0]}^3 mesh, box '
-                               f'{side * args.spacing:g} Mpc/h, 1 fwd + 1 adjoint leapfrog step '
-                               f'of a {args.nbody_steps}-step run',
-                   'ptcl': N, 'mesh_cells': M, 'parallelism': f'replicas x{world}',
-                   'l2': 'inputs larger than L2 (mesh 4.3 GB per array)'},
+        'data': DATA,
+        'config': workload_config(args, world),
         'roofline': roofline,
         'step_roofline': {'bytes_per_step': step_bytes, 'achieved': step_gbs, 'peak': peak,
                           'frac': step_gbs / peak, 'unit': 'GB/s',

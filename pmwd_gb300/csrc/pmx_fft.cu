@@ -412,12 +412,36 @@ __global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__
     cp_async_wait_all();
 }
 
-// Adjoint x pass.  The three input components of a tile rotate through three
-// buffers: while tile i is transformed, the copies of tile i+1 are issued as
-// soon as a buffer frees up (C_0 and C_1 after the fused step, C_2 after the
-// store phase), and tile i+1 waits for C_2 only after the step 1 of C_0 and
-// C_1.  B = i ky C_1 + i kz C_2 is formed after step 1 (the x transform is
-// linear and ky, kz are constant along x).
+// Loads B = i ky C_1 + i kz C_2 of a column tile (components 1, 2 of the
+// (x, 3, n1, n2h) array) synchronously, in register batches.
+template <class C>
+__device__ __forceinline__ void load_comb(const float2 *__restrict__ Cin, int64_t j, int64_t l0,
+                                          float myj, const float *__restrict__ mz,
+                                          const XGeom &g, float2 *buf) {
+    constexpr int T = C::T, XS = C::TH / C::T, PER = C::PER, CH = PER < 8 ? PER : 8;
+    const int t = threadIdx.x % T, x0 = threadIdx.x / T;
+    const int64_t l = l0 + t;
+    const bool ok = l >= 0 && l < g.n2h;
+    const float mzl = ok ? __ldg(mz + l) : 0.f;
+    const int64_t cs = g.n1 * g.n2h, xs = 3 * cs;
+    const float2 *base = Cin + j * g.n2h + (ok ? l : 0);
+#pragma unroll
+    for (int b = 0; b < PER; b += CH) {
+        float2 c1[CH], c2[CH];
+#pragma unroll
+        for (int r = 0; r < CH; ++r) {
+            const int x = x0 + (b + r) * XS;
+            c1[r] = ok ? __ldg(base + x * xs + cs) : make_float2(0.f, 0.f);
+            c2[r] = ok ? __ldg(base + x * xs + 2 * cs) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int r = 0; r < CH; ++r)  // i k (a + i b) = (-k b, k a)
+            buf[C::at(t, x0 + (b + r) * XS)] =
+                make_float2(-__fadd_rn(__fmul_rn(myj, c1[r].y), __fmul_rn(mzl, c2[r].y)),
+                            __fadd_rn(__fmul_rn(myj, c1[r].x), __fmul_rn(mzl, c2[r].x)));
+    }
+}
+
 template <int N>
 __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__ Cin,
                                                       float2 *__restrict__ S,
@@ -427,8 +451,7 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
     using C = XCfg<N, XTA>;
     constexpr int T = C::T, R1 = C::R1, R2 = C::R2;
     extern __shared__ __align__(16) float2 smem2[];
-    // buffers of C_0, C_1, C_2 of the current tile (rotated per tile)
-    float2 *A = smem2, *B = smem2 + C::BUF, *P = smem2 + 2 * C::BUF;
+    float2 *A0 = smem2, *A1 = smem2 + C::BUF, *B = smem2 + 2 * C::BUF;
     float2 *tw = smem2 + 3 * C::BUF;
     float *kxs = reinterpret_cast<float *>(tw + N), *mxs = kxs + N;
 
@@ -443,45 +466,37 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
 
     const int64_t ntiles = g.n1 * g.ncol_tiles;
     int64_t tile = blockIdx.x;
-    if (tile < ntiles) {
-        const int64_t j = g.row(tile), l0 = g.col0(tile, T);
-        issue_tile<C>(Cin, 3, 0, j, l0, g, A);
-        issue_tile<C>(Cin, 3, 1, j, l0, g, B);
-        cp_async_commit();
-        issue_tile<C>(Cin, 3, 2, j, l0, g, P);
-    }
+    if (tile < ntiles) issue_tile<C>(Cin, 3, 0, g.row(tile), g.col0(tile, T), g, A0);
     cp_async_commit();
-    for (; tile < ntiles; tile += gridDim.x) {
+    for (int cur = 0; tile < ntiles; tile += gridDim.x, cur ^= 1) {
+        float2 *A = cur ? A1 : A0;
         const int64_t j = g.row(tile);
         const int64_t l0 = g.col0(tile, T);
+        // the previous tile's store phase (reads of the other A buffer) is over
+        __syncthreads();
         const int64_t nxt = tile + gridDim.x;
-        cp_async_wait_group1();  // C_0, C_1 of this tile
+        if (nxt < ntiles) issue_tile<C>(Cin, 3, 0, g.row(nxt), g.col0(nxt, T), g, cur ? A0 : A1);
+        cp_async_commit();
+        const float myj = __ldg(my + j);
+        load_comb<C>(Cin, j, l0, myj, mz, g, B);
+        cp_async_wait_group1();  // this tile's C_0 (the next tile's may stay in flight)
         __syncthreads();
         fwd_step1<C>(A, tw);
         fwd_step1<C>(B, tw);
-        cp_async_wait_all();     // C_2
         __syncthreads();
-        fwd_step1<C>(P, tw);
-        __syncthreads();
-        const float kyj = __ldg(ky + j), myj = __ldg(my + j);
+        const float kyj = __ldg(ky + j);
         const float ky2 = __fmul_rn(kyj, kyj);
         for (int it = threadIdx.x; it < T * R1; it += XTA) {
             const int t = it / R1, k1 = it % R1;
             const int64_t l = l0 + t;
-            const bool okl = l >= 0 && l < g.n2h;
-            const float kzl = okl ? __ldg(kz + l) : 0.f, mzl = okl ? __ldg(mz + l) : 0.f;
+            const float kzl = l >= 0 && l < g.n2h ? __ldg(kz + l) : 0.f;
             const float kz2 = __fmul_rn(kzl, kzl);
-            const int q0 = t * C::CS + k1 * (R2 + 1);
             float2 v[R2], w[R2];
 #pragma unroll
-            for (int b = 0; b < R2; ++b) v[b] = A[q0 + b];
+            for (int b = 0; b < R2; ++b) v[b] = A[t * C::CS + k1 * (R2 + 1) + b];
             dft2<R2, false>(v);
 #pragma unroll
-            for (int b = 0; b < R2; ++b) {  // i ky C_1 + i kz C_2; i k (a + i b) = (-k b, k a)
-                const float2 c1 = B[q0 + b], c2 = P[q0 + b];
-                w[b] = make_float2(-__fadd_rn(__fmul_rn(myj, c1.y), __fmul_rn(mzl, c2.y)),
-                                   __fadd_rn(__fmul_rn(myj, c1.x), __fmul_rn(mzl, c2.x)));
-            }
+            for (int b = 0; b < R2; ++b) w[b] = B[t * C::CS + k1 * (R2 + 1) + b];
             dft2<R2, false>(w);
 #pragma unroll
             for (int k = 0; k < R2; ++k) {
@@ -495,12 +510,7 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
             }
             inv_step2_store<C>(v, A, t, k1, tw);
         }
-        __syncthreads();  // B and P are free: next tile's C_0 into P, C_1 into B
-        if (nxt < ntiles) {
-            issue_tile<C>(Cin, 3, 0, g.row(nxt), g.col0(nxt, T), g, P);
-            issue_tile<C>(Cin, 3, 1, g.row(nxt), g.col0(nxt, T), g, B);
-        }
-        cp_async_commit();
+        __syncthreads();
         inv_step1<C>(A);
         __syncthreads();
         {
@@ -513,12 +523,6 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
                 for (int x = threadIdx.x / T; x < N; x += XS) o[x * xs] = A[C::at(t, x)];
             }
         }
-        __syncthreads();  // A is free: next tile's C_2
-        if (nxt < ntiles) issue_tile<C>(Cin, 3, 2, g.row(nxt), g.col0(nxt, T), g, A);
-        cp_async_commit();
-        float2 *const A0 = A;  // next tile: C_0 in P, C_1 in B, C_2 in A
-        A = P;
-        P = A0;
     }
     cp_async_wait_all();
 }
