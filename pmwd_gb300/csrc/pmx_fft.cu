@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include <utility>
 
@@ -278,26 +279,27 @@ __device__ __forceinline__ void inv_step2_store(float2 (&v)[C::R2], float2 *buf,
 }
 
 // Column tiles of a ky row j start at l0 = s_j + (k - 1) T, k < ncol_tiles,
-// with s_j = (-j n2h) mod 4: every tile but the first and last of a row then
-// covers whole 32-byte sectors of every x-plane (the plane size n1 n2h is a
-// multiple of 4 then).  HBM3e has no byte-masked writes, so partial-sector
+// with s_j = (-j rs) mod 4 (rs the row stride): every tile but the first and
+// last of a row then covers whole 32-byte sectors of every x-plane (the plane
+// size n1 rs is a multiple of 4 then).  HBM3e has no byte-masked writes, so partial-sector
 // stores would cost read-modify-writes.  Columns outside [0, n2h) are idle.
 struct XGeom {
     int64_t n1, n2h;
+    int64_t rs;           // row stride of the complex arrays (>= n2h)
     int64_t ncol_tiles;   // ceil(n2h / T) + 1
-    int align;            // 1: shift rows as above (n1 n2h % 4 == 0)
+    int align;            // 1: shift rows as above (n1 rs % 4 == 0)
     float c;              // 1.5 Omega_m / N
     __device__ __forceinline__ int64_t row(int64_t tile) const { return tile / ncol_tiles; }
     __device__ __forceinline__ int64_t col0(int64_t tile, int T) const {
         const int64_t j = tile / ncol_tiles, k = tile % ncol_tiles;
-        const int64_t sj = align ? (4 - (j * n2h) % 4) % 4 : 0;
+        const int64_t sj = align ? (4 - (j * rs) % 4) % 4 : 0;
         return sj + (k - 1) * T;
     }
 };
 
 // Starts the asynchronous load of the column tile (fixed ky row j, kz in
 // [l0, l0+T), all x) of component `comp` of a complex array laid out
-// (x, ncomp, n1, n2h); columns past n2h read as zero.
+// (x, ncomp, n1, rs); columns outside [0, n2h) read as zero.
 template <class C>
 __device__ __forceinline__ void issue_tile(const float2 *__restrict__ src, int ncomp, int comp,
                                            int64_t j, int64_t l0, const XGeom &g, float2 *buf) {
@@ -305,8 +307,8 @@ __device__ __forceinline__ void issue_tile(const float2 *__restrict__ src, int n
     const int t = threadIdx.x % T, x0 = threadIdx.x / T;
     const int64_t l = l0 + t;
     const bool ok = l >= 0 && l < g.n2h;
-    const float2 *base = src + ((int64_t)comp * g.n1 + j) * g.n2h + (ok ? l : 0);
-    const int64_t xs = (int64_t)ncomp * g.n1 * g.n2h;
+    const float2 *base = src + ((int64_t)comp * g.n1 + j) * g.rs + (ok ? l : 0);
+    const int64_t xs = (int64_t)ncomp * g.n1 * g.rs;
 #pragma unroll 8
     for (int r = 0; r < C::PER; ++r) {
         const int x = x0 + r * XS;
@@ -389,15 +391,15 @@ __global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__
         inv_step1<C>(A);
         inv_step1<C>(B);
         __syncthreads();
-        // G_0 = B; G_1 = -i ky Q; G_2 = -i kz Q  (Q in A); layout (x, 3, n1, n2h)
+        // G_0 = B; G_1 = -i ky Q; G_2 = -i kz Q  (Q in A); layout (x, 3, n1, rs)
         {
             constexpr int XS = XTF / T;
             const int t = threadIdx.x % T;
             const int64_t l = l0 + t;
             if (l >= 0 && l < g.n2h) {
                 const float mzl = __ldg(mz + l);
-                const int64_t cs = g.n1 * g.n2h, xs = 3 * cs;
-                float2 *o = G + j * g.n2h + l;
+                const int64_t cs = g.n1 * g.rs, xs = 3 * cs;
+                float2 *o = G + j * g.rs + l;
                 for (int x = threadIdx.x / T; x < N; x += XS) {
                     const int q = C::at(t, x);
                     const float2 Q = A[q];
@@ -413,7 +415,7 @@ __global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__
 }
 
 // Loads B = i ky C_1 + i kz C_2 of a column tile (components 1, 2 of the
-// (x, 3, n1, n2h) array) synchronously, in register batches.
+// (x, 3, n1, rs) array) synchronously, in register batches.
 template <class C>
 __device__ __forceinline__ void load_comb(const float2 *__restrict__ Cin, int64_t j, int64_t l0,
                                           float myj, const float *__restrict__ mz,
@@ -423,8 +425,8 @@ __device__ __forceinline__ void load_comb(const float2 *__restrict__ Cin, int64_
     const int64_t l = l0 + t;
     const bool ok = l >= 0 && l < g.n2h;
     const float mzl = ok ? __ldg(mz + l) : 0.f;
-    const int64_t cs = g.n1 * g.n2h, xs = 3 * cs;
-    const float2 *base = Cin + j * g.n2h + (ok ? l : 0);
+    const int64_t cs = g.n1 * g.rs, xs = 3 * cs;
+    const float2 *base = Cin + j * g.rs + (ok ? l : 0);
 #pragma unroll
     for (int b = 0; b < PER; b += CH) {
         float2 c1[CH], c2[CH];
@@ -518,8 +520,8 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
             const int t = threadIdx.x % T;
             const int64_t l = l0 + t;
             if (l >= 0 && l < g.n2h) {
-                float2 *o = S + j * g.n2h + l;
-                const int64_t xs = g.n1 * g.n2h;
+                float2 *o = S + j * g.rs + l;
+                const int64_t xs = g.n1 * g.rs;
                 for (int x = threadIdx.x / T; x < N; x += XS) o[x * xs] = A[C::at(t, x)];
             }
         }
@@ -537,17 +539,18 @@ size_t xpass_smem(bool adj) {
 
 template <int N>
 int launch_xpass(bool adj, const float2 *in, float2 *out, const float *kt, const float2 *tw,
-                 int64_t n1, int64_t n2h, float c, cudaStream_t st) {
+                 int64_t n1, int64_t n2h, int64_t rs, float c, cudaStream_t st) {
     XGeom g;
     g.n1 = n1;
     g.n2h = n2h;
+    g.rs = rs;
     g.c = c;
     const size_t sm = xpass_smem<N>(adj);
     const void *fn = adj ? (const void *)k_xpass_adj<N> : (const void *)k_xpass_fwd<N>;
     const int threads = adj ? XTA : XTF;
     const int T = adj ? XCfg<N, XTA>::T : XCfg<N, XTF>::T;
     g.ncol_tiles = (n2h + T - 1) / T + 1;
-    g.align = (n1 * n2h) % 4 == 0;
+    g.align = (n1 * rs) % 4 == 0;
     PMX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     int per_sm = 0;
     PMX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, sm));
@@ -569,13 +572,20 @@ int launch_xpass(bool adj, const float2 *in, float2 *out, const float *kt, const
 // Plane (y, z) transforms.  The 3-D r2c / c2r transforms of the force are
 // the x pass above plus, per x-plane (and component), a 2-D transform over
 // (y, z): real rows of n2 values along z (contiguous) and complex columns of
-// n1 values along y (stride n2h).  One thread-block cluster of PCL CTAs owns
-// a plane at a time: each CTA transforms n1/PCL rows, the cluster
-// synchronises (barrier.cluster: release/acquire at cluster scope, so the
-// rows written by the other CTAs are visible), then each CTA transforms
-// every PCL-th tile of T columns in place.  Between the two phases the plane
-// (n1 * n2h * 8 bytes, 4.2 MB at 1024^2) sits in L2, so HBM sees one read
-// of the input and one write of the output per plane.
+// n1 values along y.  Complex rows are stored at the padded stride
+// RS = padded_row(n2h), so every 8-column tile covers whole 32-byte sectors.
+// One thread-block cluster of CL CTAs owns a plane at a time: each CTA
+// transforms n1/CL rows, the cluster synchronises (barrier.cluster:
+// release/acquire at cluster scope, so the rows written by the other CTAs
+// are visible), then each CTA transforms every CL-th tile of T columns.
+// Between the two phases the plane (n1 * RS * 8 bytes, 4.2 MB at 1024^2)
+// sits in L2, so HBM sees one read of the input and one write of the output
+// per plane:
+//   r2c: rows -> the output plane (stores marked L2 evict_last), columns in
+//        place (the final stores evict_first);
+//   c2r: columns of the input -> a per-cluster scratch plane that is
+//        rewritten for every plane (evict_last: it stays in L2 and is never
+//        written back), rows of the scratch -> the real output (evict_first).
 //
 // Rows use the half-length complex FFT: z[m] = x[2m] + i x[2m+1],
 // Z = FFT_L(z) (L = n2/2), then X[k] = E[k] + w_N^k O[k] with
@@ -588,7 +598,32 @@ int launch_xpass(bool adj, const float2 *in, float2 *out, const float *kt, const
 namespace cg = cooperative_groups;
 
 constexpr int PTH = 256;  // threads per plane CTA
-constexpr int PCL = 8;    // CTAs per plane cluster
+
+// L2 cache policies (createpolicy) for the eviction-priority hints.
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+    return p;
+}
+// cp_async8 with an L2 eviction policy
+__device__ __forceinline__ void cp_async8_pol(float2 *dst, const float2 *src, bool ok, uint64_t pol) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int n = ok ? 8 : 0;
+    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2, %3;\n" ::"r"(d),
+                 "l"(src), "r"(n), "l"(pol)
+                 : "memory");
+}
+// 8-byte global store with an L2 eviction policy
+__device__ __forceinline__ void st8_pol(float2 *p, float2 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;\n" ::"l"(p), "f"(v.x),
+                 "f"(v.y), "l"(pol)
+                 : "memory");
+}
 
 // Length-N FFT (N = R1 * R2) of the T columns of a padded tile buffer, in
 // place, natural order in and out; INV selects exp(+2 pi i ...).  Step 2
@@ -627,10 +662,10 @@ __device__ __forceinline__ void fft_cols(float2 *buf, const float2 *tw) {
 }
 
 // Asynchronous load of T columns [l0, l0+T) (those < ncol valid, the rest
-// zero) of `rows` rows with row stride `rs` (float2) into a tile buffer.
+// zero) of ROWS rows with row stride rs (float2) into a tile buffer.
 template <class C, int ROWS>
 __device__ __forceinline__ void issue_cols(const float2 *src, int64_t rs, int l0, int ncol,
-                                           float2 *buf) {
+                                           float2 *buf, uint64_t pol) {
     constexpr int T = C::T, XS = C::TH / C::T;
     const int t = threadIdx.x % T, y0 = threadIdx.x / T;
     const bool ok = l0 + t < ncol;
@@ -638,35 +673,42 @@ __device__ __forceinline__ void issue_cols(const float2 *src, int64_t rs, int l0
 #pragma unroll 8
     for (int r = 0; r < ROWS / XS; ++r) {
         const int y = y0 + r * XS;
-        cp_async8(buf + C::at(t, y), base + y * rs, ok);
+        cp_async8_pol(buf + C::at(t, y), base + y * rs, ok, pol);
     }
 }
 
-// Stores T columns of a tile buffer back (columns >= ncol skipped).
+// Stores T columns of a tile buffer (columns >= ncol skipped).
 template <class C, int ROWS>
 __device__ __forceinline__ void store_cols(float2 *dst, int64_t rs, int l0, int ncol,
-                                           const float2 *buf) {
-    constexpr int T = C::T;
-    for (int it = threadIdx.x; it < ROWS * T; it += C::TH) {
-        const int t = it % T, y = it / T;
-        if (l0 + t < ncol) dst[(int64_t)y * rs + l0 + t] = buf[C::at(t, y)];
-    }
+                                           const float2 *buf, uint64_t pol) {
+    constexpr int T = C::T, XS = C::TH / C::T;
+    const int t = threadIdx.x % T;
+    if (l0 + t >= ncol) return;
+    for (int y = threadIdx.x / T; y < ROWS; y += XS)
+        st8_pol(dst + (int64_t)y * rs + l0 + t, buf[C::at(t, y)], pol);
 }
 
 struct PGeom {
     int64_t nplanes;
+    float2 *scratch;  // c2r: one plane (N1 x RS complex) per cluster
 };
 
-// Forward plane transform: real planes (n1, 2L) -> complex planes (n1, L+1).
+template <int L>
+struct PRow {
+    static constexpr int N2H = L + 1;
+    static constexpr int RS = (N2H + 3) & ~3;  // padded_row(N2H)
+};
+
+// Forward plane transform: real planes (n1, 2L) -> complex planes (n1, RS).
 // Twiddles in ptw: [exp(-2 pi i m / N1), m < N1 | exp(-2 pi i m / L), m < L |
 // exp(-2 pi i k / 2L), k <= L].
-template <int N1, int L>
+template <int N1, int L, int CL>
 __global__ void __launch_bounds__(PTH, 1) k_plane_r2c(const float *__restrict__ in,
                                                       float2 *__restrict__ out,
                                                       const float2 *__restrict__ ptw, PGeom g) {
     using ZC = XCfg<L, PTH>;
     using YC = XCfg<N1, PTH>;
-    constexpr int N2 = 2 * L, N2H = L + 1, RPC = N1 / PCL;
+    constexpr int N2 = 2 * L, N2H = L + 1, RS = PRow<L>::RS, RPC = N1 / CL;
     constexpr int ZT = ZC::T, NB = (RPC + ZT - 1) / ZT;
     constexpr int YT = YC::T, NTILE = (N2H + YT - 1) / YT;
     constexpr int ZREG = 2 * ZC::BUF, YREG = 2 * YC::BUF;
@@ -674,21 +716,23 @@ __global__ void __launch_bounds__(PTH, 1) k_plane_r2c(const float *__restrict__ 
     extern __shared__ __align__(16) float2 smem2[];
     float2 *twY = smem2 + REG, *twL = twY + N1, *twN = twL + L;
     for (int m = threadIdx.x; m < N1 + L + N2H; m += PTH) twY[m] = ptw[m];
+    const uint64_t pfirst = policy_evict_first(), plast = policy_evict_last();
 
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
-    const int64_t cid = blockIdx.x / PCL, ncl = gridDim.x / PCL;
+    const int64_t cid = blockIdx.x / CL, ncl = gridDim.x / CL;
     const int yb = rank * RPC;
 
     for (int64_t p = cid; p < g.nplanes; p += ncl) {
         const float2 *src = reinterpret_cast<const float2 *>(in + p * (int64_t)N1 * N2);
-        float2 *dst = out + p * (int64_t)N1 * N2H;
+        float2 *dst = out + p * (int64_t)N1 * RS;
         // rows [yb, yb + RPC): half-length FFT, then the real-input split
         auto issue_rows = [&](int b, float2 *buf) {
             for (int it = threadIdx.x; it < ZT * L; it += PTH) {
                 const int t = it / L, m = it % L, y = b * ZT + t;
                 const bool ok = y < RPC;
-                cp_async8(buf + ZC::at(t, m), src + (int64_t)(yb + (ok ? y : 0)) * L + m, ok);
+                cp_async8_pol(buf + ZC::at(t, m), src + (int64_t)(yb + (ok ? y : 0)) * L + m, ok,
+                              pfirst);
             }
         };
         issue_rows(0, smem2);
@@ -708,40 +752,42 @@ __global__ void __launch_bounds__(PTH, 1) k_plane_r2c(const float *__restrict__ 
                 const float2 e = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
                 const float2 o = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
                 const float2 w = twN[k];
-                dst[(int64_t)(yb + y) * N2H + k] =
-                    make_float2(e.x + (w.x * o.x - w.y * o.y), e.y + (w.x * o.y + w.y * o.x));
+                st8_pol(dst + (int64_t)(yb + y) * RS + k,
+                        make_float2(e.x + (w.x * o.x - w.y * o.y), e.y + (w.x * o.y + w.y * o.x)),
+                        plast);
             }
         }
         cp_async_wait_all();
         cl.sync();  // every row of the plane is written (and visible)
-        // columns: tiles rank, rank + PCL, ...
+        // columns in place: tiles rank, rank + CL, ...
         int tl = rank;
-        if (tl < NTILE) issue_cols<YC, N1>(dst, N2H, tl * YT, N2H, smem2);
+        if (tl < NTILE) issue_cols<YC, N1>(dst, RS, tl * YT, N2H, smem2, pfirst);
         cp_async_commit();
-        for (int i = 0; tl < NTILE; tl += PCL, ++i) {
+        for (int i = 0; tl < NTILE; tl += CL, ++i) {
             float2 *buf = smem2 + (i & 1) * YC::BUF;
             cp_async_wait_all();
             __syncthreads();
-            if (tl + PCL < NTILE)
-                issue_cols<YC, N1>(dst, N2H, (tl + PCL) * YT, N2H, smem2 + ((i + 1) & 1) * YC::BUF);
+            if (tl + CL < NTILE)
+                issue_cols<YC, N1>(dst, RS, (tl + CL) * YT, N2H, smem2 + ((i + 1) & 1) * YC::BUF,
+                                   pfirst);
             cp_async_commit();
             fft_cols<YC, false>(buf, twY);
-            store_cols<YC, N1>(dst, N2H, tl * YT, N2H, buf);
+            store_cols<YC, N1>(dst, RS, tl * YT, N2H, buf, pfirst);
         }
         cp_async_wait_all();
         __syncthreads();  // tile buffers free before the next plane's rows
     }
 }
 
-// Inverse plane transform: complex planes (n1, L+1) -> real planes (n1, 2L).
-// The complex input is transformed in place along y first (destroyed).
-template <int N1, int L>
-__global__ void __launch_bounds__(PTH, 1) k_plane_c2r(float2 *__restrict__ in,
+// Inverse plane transform: complex planes (n1, RS) -> real planes (n1, 2L),
+// through the cluster's scratch plane (the input is left unchanged).
+template <int N1, int L, int CL>
+__global__ void __launch_bounds__(PTH, 1) k_plane_c2r(const float2 *__restrict__ in,
                                                       float *__restrict__ out,
                                                       const float2 *__restrict__ ptw, PGeom g) {
     using ZC = XCfg<L, PTH>;
     using YC = XCfg<N1, PTH>;
-    constexpr int N2 = 2 * L, N2H = L + 1, RPC = N1 / PCL;
+    constexpr int N2 = 2 * L, N2H = L + 1, RS = PRow<L>::RS, RPC = N1 / CL;
     constexpr int ZT = ZC::T, NB = (RPC + ZT - 1) / ZT;
     constexpr int YT = YC::T, NTILE = (N2H + YT - 1) / YT;
     constexpr int XRS = N2H + 1;  // raw row stride in shared memory
@@ -750,38 +796,42 @@ __global__ void __launch_bounds__(PTH, 1) k_plane_c2r(float2 *__restrict__ in,
     extern __shared__ __align__(16) float2 smem2[];
     float2 *twY = smem2 + REG, *twL = twY + N1, *twN = twL + L;
     for (int m = threadIdx.x; m < N1 + L + N2H; m += PTH) twY[m] = ptw[m];
+    const uint64_t pfirst = policy_evict_first(), plast = policy_evict_last();
 
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
-    const int64_t cid = blockIdx.x / PCL, ncl = gridDim.x / PCL;
+    const int64_t cid = blockIdx.x / CL, ncl = gridDim.x / CL;
     const int yb = rank * RPC;
+    float2 *scr = g.scratch + cid * (int64_t)N1 * RS;
 
     for (int64_t p = cid; p < g.nplanes; p += ncl) {
-        float2 *cpl = in + p * (int64_t)N1 * N2H;
+        const float2 *cpl = in + p * (int64_t)N1 * RS;
         float2 *rpl = reinterpret_cast<float2 *>(out + p * (int64_t)N1 * N2);
-        // columns first (inverse along y, in place)
+        // columns first (inverse along y) into the scratch plane
         int tl = rank;
-        if (tl < NTILE) issue_cols<YC, N1>(cpl, N2H, tl * YT, N2H, smem2);
+        if (tl < NTILE) issue_cols<YC, N1>(cpl, RS, tl * YT, N2H, smem2, pfirst);
         cp_async_commit();
-        for (int i = 0; tl < NTILE; tl += PCL, ++i) {
+        for (int i = 0; tl < NTILE; tl += CL, ++i) {
             float2 *buf = smem2 + (i & 1) * YC::BUF;
             cp_async_wait_all();
             __syncthreads();
-            if (tl + PCL < NTILE)
-                issue_cols<YC, N1>(cpl, N2H, (tl + PCL) * YT, N2H, smem2 + ((i + 1) & 1) * YC::BUF);
+            if (tl + CL < NTILE)
+                issue_cols<YC, N1>(cpl, RS, (tl + CL) * YT, N2H, smem2 + ((i + 1) & 1) * YC::BUF,
+                                   pfirst);
             cp_async_commit();
             fft_cols<YC, true>(buf, twY);
-            store_cols<YC, N1>(cpl, N2H, tl * YT, N2H, buf);
+            store_cols<YC, N1>(scr, RS, tl * YT, N2H, buf, plast);
         }
         cp_async_wait_all();
-        cl.sync();  // every column of the plane is transformed (and visible)
+        cl.sync();  // every column of the plane is in the scratch (and visible)
         // rows [yb, yb + RPC): Hermitian rebuild, half-length inverse FFT
         float2 *F = smem2 + 2 * ZT * XRS;
         auto issue_rows = [&](int b, float2 *raw) {
             for (int it = threadIdx.x; it < ZT * N2H; it += PTH) {
                 const int t = it / N2H, k = it % N2H, y = b * ZT + t;
                 const bool ok = y < RPC;
-                cp_async8(raw + t * XRS + k, cpl + (int64_t)(yb + (ok ? y : 0)) * N2H + k, ok);
+                cp_async8_pol(raw + t * XRS + k, scr + (int64_t)(yb + (ok ? y : 0)) * RS + k, ok,
+                              plast);
             }
         };
         issue_rows(0, smem2);
@@ -809,11 +859,12 @@ __global__ void __launch_bounds__(PTH, 1) k_plane_c2r(float2 *__restrict__ in,
             fft_cols<ZC, true>(F, twL);
             for (int it = threadIdx.x; it < ZT * L; it += PTH) {
                 const int t = it / L, m = it % L, y = b * ZT + t;
-                if (y < RPC) rpl[(int64_t)(yb + y) * L + m] = F[ZC::at(t, m)];
+                if (y < RPC) st8_pol(rpl + (int64_t)(yb + y) * L + m, F[ZC::at(t, m)], pfirst);
             }
         }
         cp_async_wait_all();
-        __syncthreads();
+        // the scratch rows are read: the cluster may overwrite it next plane
+        cl.sync();
     }
 }
 
@@ -827,36 +878,49 @@ size_t plane_smem(bool inv) {
     return (size_t)(reg + N1 + L + L + 1) * sizeof(float2);
 }
 
-template <int N1, int L>
-int launch_plane(bool inv, const void *in, void *out, const float2 *ptw, int64_t nplanes,
-                 cudaStream_t st) {
+template <int N1, int L, int CL>
+cudaError_t plane_config(bool inv, cudaLaunchConfig_t *cfg, cudaLaunchAttribute *attr, int *ncl) {
     const size_t sm = plane_smem<N1, L>(inv);
-    const void *fn = inv ? (const void *)k_plane_c2r<N1, L> : (const void *)k_plane_r2c<N1, L>;
-    PMX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
+    const void *fn = inv ? (const void *)k_plane_c2r<N1, L, CL> : (const void *)k_plane_r2c<N1, L, CL>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e == cudaSuccess && CL > 8)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    *cfg = cudaLaunchConfig_t{};
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = PCL;
+    attr[0].val.clusterDim.x = CL;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(PTH);
-    cfg.dynamicSmemBytes = sm;
-    cfg.stream = st;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cfg.gridDim = dim3(PCL);
+    cfg->blockDim = dim3(PTH);
+    cfg->dynamicSmemBytes = sm;
+    cfg->attrs = attr;
+    cfg->numAttrs = 1;
+    cfg->gridDim = dim3(CL);
+    return cudaOccupancyMaxActiveClusters(ncl, fn, cfg);
+}
+
+template <int N1, int L, int CL>
+int launch_plane(bool inv, const void *in, void *out, const float2 *ptw, int64_t nplanes,
+                 float2 *scratch, int max_clusters, cudaStream_t st) {
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
     int ncl = 0;
-    PMX_CUDA(cudaOccupancyMaxActiveClusters(&ncl, fn, &cfg));
+    PMX_CUDA((plane_config<N1, L, CL>(inv, &cfg, attr, &ncl)));
     if (ncl < 1) return fail(PMX_ERR_CUDA, "plane transform cluster does not fit on the GPU");
+    if (ncl > max_clusters) ncl = max_clusters;
     if (ncl > nplanes) ncl = (int)nplanes;
-    cfg.gridDim = dim3(ncl * PCL);
+    cfg.gridDim = dim3(ncl * CL);
+    cfg.stream = st;
     PGeom g;
     g.nplanes = nplanes;
+    g.scratch = scratch;
     if (inv) {
-        PMX_CUDA(cudaLaunchKernelEx(&cfg, k_plane_c2r<N1, L>, (float2 *)in, (float *)out, ptw, g));
+        PMX_CUDA(cudaLaunchKernelEx(&cfg, k_plane_c2r<N1, L, CL>, (const float2 *)in, (float *)out,
+                                    ptw, g));
         PMX_LAUNCH_CHECK("k_plane_c2r");
     } else {
-        PMX_CUDA(cudaLaunchKernelEx(&cfg, k_plane_r2c<N1, L>, (const float *)in, (float2 *)out, ptw, g));
+        PMX_CUDA(cudaLaunchKernelEx(&cfg, k_plane_r2c<N1, L, CL>, (const float *)in, (float2 *)out,
+                                    ptw, g));
         PMX_LAUNCH_CHECK("k_plane_r2c");
     }
     return PMX_OK;
@@ -869,13 +933,13 @@ bool xpass_supported(int64_t n0) {
 }
 
 int xpass(bool adj, const float2 *in, float2 *out, const float *kt, const float2 *tw, int64_t n0,
-          int64_t n1, int64_t n2h, float c, cudaStream_t st) {
+          int64_t n1, int64_t n2h, int64_t rs, float c, cudaStream_t st) {
     switch (n0) {
-        case 64: return launch_xpass<64>(adj, in, out, kt, tw, n1, n2h, c, st);
-        case 128: return launch_xpass<128>(adj, in, out, kt, tw, n1, n2h, c, st);
-        case 256: return launch_xpass<256>(adj, in, out, kt, tw, n1, n2h, c, st);
-        case 512: return launch_xpass<512>(adj, in, out, kt, tw, n1, n2h, c, st);
-        case 1024: return launch_xpass<1024>(adj, in, out, kt, tw, n1, n2h, c, st);
+        case 64: return launch_xpass<64>(adj, in, out, kt, tw, n1, n2h, rs, c, st);
+        case 128: return launch_xpass<128>(adj, in, out, kt, tw, n1, n2h, rs, c, st);
+        case 256: return launch_xpass<256>(adj, in, out, kt, tw, n1, n2h, rs, c, st);
+        case 512: return launch_xpass<512>(adj, in, out, kt, tw, n1, n2h, rs, c, st);
+        case 1024: return launch_xpass<1024>(adj, in, out, kt, tw, n1, n2h, rs, c, st);
         default: return fail(PMX_ERR_SHAPE, "x-pass needs n0 in {64, 128, 256, 512, 1024}");
     }
 }
@@ -893,17 +957,57 @@ bool plane_supported(int64_t n1, int64_t n2) {
     return n1 == n2 && (n1 == 64 || n1 == 128 || n1 == 256 || n1 == 512 || n1 == 1024);
 }
 
+// Cluster size of the plane kernels: PMX_PLANE_CLUSTER (8 or 16), else 8.
+int plane_cluster() {
+    const char *e = std::getenv("PMX_PLANE_CLUSTER");
+    return e && std::atoi(e) == 16 ? 16 : 8;
+}
+
+int plane_max_clusters(int64_t n1, int64_t n2, int *ncl) {
+    if (!plane_supported(n1, n2)) return fail(PMX_ERR_SHAPE, "plane transform needs square power-of-two planes 64..1024");
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    const bool c16 = plane_cluster() == 16;
+    int a = 0, b = 0;
+    cudaError_t e = cudaSuccess;
+#define PMX_PLANE_Q(N1_, L_)                                                                       \
+    if (c16) {                                                                                      \
+        e = plane_config<N1_, L_, 16>(false, &cfg, attr, &a);                                       \
+        if (e == cudaSuccess) e = plane_config<N1_, L_, 16>(true, &cfg, attr, &b);                  \
+    } else {                                                                                        \
+        e = plane_config<N1_, L_, 8>(false, &cfg, attr, &a);                                        \
+        if (e == cudaSuccess) e = plane_config<N1_, L_, 8>(true, &cfg, attr, &b);                   \
+    }
+    switch (n1) {
+        case 64: PMX_PLANE_Q(64, 32) break;
+        case 128: PMX_PLANE_Q(128, 64) break;
+        case 256: PMX_PLANE_Q(256, 128) break;
+        case 512: PMX_PLANE_Q(512, 256) break;
+        default: PMX_PLANE_Q(1024, 512) break;
+    }
+#undef PMX_PLANE_Q
+    if (e != cudaSuccess) return cuda_status(e, "plane kernel occupancy");
+    *ncl = a > b ? a : b;
+    if (*ncl < 1) return fail(PMX_ERR_CUDA, "plane transform cluster does not fit on the GPU");
+    return PMX_OK;
+}
+
 int plane_fft(bool inv, const void *in, void *out, const float2 *ptw, int64_t nplanes, int64_t n1,
-              int64_t n2, cudaStream_t st) {
+              int64_t n2, float2 *scratch, int max_clusters, cudaStream_t st) {
     if (!plane_supported(n1, n2)) return fail(PMX_ERR_SHAPE, "plane transform needs square power-of-two planes 64..1024");
     if (nplanes < 1) return PMX_OK;
+    const bool c16 = plane_cluster() == 16;
+#define PMX_PLANE_L(N1_, L_)                                                                       \
+    return c16 ? launch_plane<N1_, L_, 16>(inv, in, out, ptw, nplanes, scratch, max_clusters, st)  \
+               : launch_plane<N1_, L_, 8>(inv, in, out, ptw, nplanes, scratch, max_clusters, st);
     switch (n1) {
-        case 64: return launch_plane<64, 32>(inv, in, out, ptw, nplanes, st);
-        case 128: return launch_plane<128, 64>(inv, in, out, ptw, nplanes, st);
-        case 256: return launch_plane<256, 128>(inv, in, out, ptw, nplanes, st);
-        case 512: return launch_plane<512, 256>(inv, in, out, ptw, nplanes, st);
-        default: return launch_plane<1024, 512>(inv, in, out, ptw, nplanes, st);
+        case 64: PMX_PLANE_L(64, 32)
+        case 128: PMX_PLANE_L(128, 64)
+        case 256: PMX_PLANE_L(256, 128)
+        case 512: PMX_PLANE_L(512, 256)
+        default: PMX_PLANE_L(1024, 512)
     }
+#undef PMX_PLANE_L
 }
 
 // [exp(-2 pi i m / n1), m < n1 | exp(-2 pi i m / L), m < L | exp(-2 pi i k / n2), k <= L],

@@ -103,6 +103,9 @@ struct pmx_workspace {
     // plane kernels of pmx_fft.cu instead of 2-D cuFFT
     bool plane = false;
     float2 *ptw = nullptr;      // plane_twiddles(n1, n2)
+    float2 *pscr = nullptr;     // c2r scratch: one n1 x n2p plane per cluster
+    int pcl = 0;                // clusters the scratch serves
+    int64_t n2p = 0;            // complex row stride: padded_row(n2h) for the plane kernels
     // slab-wise 2-D cuFFT: kinds 0..3 = r2c of the density, c2r of the three
     // gradient spectra, r2c of the three mesh cotangents, c2r of the adjoint
     SlabXf sx[4];
@@ -988,7 +991,8 @@ int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t s
         float2 *H = reinterpret_cast<float2 *>(ws->g);  // g is free until the c2r
         if (ws->plane) {
             Stage sg(ws, 2, st, 1);
-            int st2 = plane_fft(false, ws->dens, H, ws->ptw, ws->n0, ws->n1, ws->n2, st);
+            int st2 = plane_fft(false, ws->dens, H, ws->ptw, ws->n0, ws->n1, ws->n2, ws->pscr,
+                                ws->pcl, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 2, st, 0);
@@ -997,12 +1001,14 @@ int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t s
         }
         {
             Stage sg(ws, 3, st, 1);
-            int st2 = xpass(false, H, ws->ck, ws->ktab, ws->tw, ws->n0, ws->n1, ws->n2h, c, st);
+            int st2 = xpass(false, H, ws->ck, ws->ktab, ws->tw, ws->n0, ws->n1, ws->n2h, ws->n2p, c,
+                            st);
             if (st2) return st2;
         }
         if (ws->plane) {
             Stage sg(ws, 4, st, 1);
-            int st2 = plane_fft(true, ws->ck, ws->g, ws->ptw, 3 * ws->n0, ws->n1, ws->n2, st);
+            int st2 = plane_fft(true, ws->ck, ws->g, ws->ptw, 3 * ws->n0, ws->n1, ws->n2, ws->pscr,
+                                ws->pcl, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 4, st, 0);
@@ -1040,7 +1046,8 @@ int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
         float2 *Sk = reinterpret_cast<float2 *>(ws->g);  // g is dead after k_g3adj
         if (ws->plane) {
             Stage sg(ws, 8, st, 1);
-            int st2 = plane_fft(false, ws->mcot, ws->ck, ws->ptw, 3 * ws->n0, ws->n1, ws->n2, st);
+            int st2 = plane_fft(false, ws->mcot, ws->ck, ws->ptw, 3 * ws->n0, ws->n1, ws->n2,
+                                ws->pscr, ws->pcl, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 8, st, 0);
@@ -1049,12 +1056,14 @@ int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
         }
         {
             Stage sg(ws, 9, st, 1);
-            int st2 = xpass(true, ws->ck, Sk, ws->ktab, ws->tw, ws->n0, ws->n1, ws->n2h, c, st);
+            int st2 = xpass(true, ws->ck, Sk, ws->ktab, ws->tw, ws->n0, ws->n1, ws->n2h, ws->n2p, c,
+                            st);
             if (st2) return st2;
         }
         if (ws->plane) {
             Stage sg(ws, 10, st, 1);
-            int st2 = plane_fft(true, Sk, ws->dens, ws->ptw, ws->n0, ws->n1, ws->n2, st);
+            int st2 = plane_fft(true, Sk, ws->dens, ws->ptw, ws->n0, ws->n1, ws->n2, ws->pscr,
+                                ws->pcl, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 10, st, 0);
@@ -1144,6 +1153,7 @@ void ws_free(pmx_workspace *ws) {
     if (ws->fork) cudaEventDestroy(ws->fork);
     cudaFree(ws->tw);
     cudaFree(ws->ptw);
+    cudaFree(ws->pscr);
     cudaFree(ws->dens);
     cudaFree(ws->ck);
     cudaFree(ws->g);
@@ -1219,8 +1229,15 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
         }
         return PMX_OK;
     };
+    const char *xenv = std::getenv("PMX_XFAST");
+    ws->xfast = xpass_supported(ws->n0) && !(flags & PMX_WS_CUFFT3D) && !(xenv && xenv[0] == '0');
+    const char *penv = std::getenv("PMX_PLANE");
+    ws->plane = ws->xfast && plane_supported(ws->n1, ws->n2) &&
+                ((flags & PMX_WS_PLANE) || (penv && penv[0] == '1')) && !(penv && penv[0] == '0');
+    ws->n2p = ws->plane ? padded_row(ws->n2h) : ws->n2h;
     int64_t ktn = 2 * (ws->n0 + ws->n1 + ws->n2h);
-    if ((st = alloc((void **)&ws->dens, ws->M * 4)) || (st = alloc((void **)&ws->ck, ws->Mc * 8 * 3)) ||
+    if ((st = alloc((void **)&ws->dens, ws->M * 4)) ||
+        (st = alloc((void **)&ws->ck, ws->n0 * ws->n1 * ws->n2p * 8 * 3)) ||
         (st = alloc((void **)&ws->g, ws->M * 4 * 3)) || (st = alloc((void **)&ws->ktab, ktn * 4)) ||
         (st = alloc((void **)&ws->part, NSLOT * PMAX * 8)) ||
         ((flags & PMX_WS_ADJOINT) && (st = alloc((void **)&ws->mcot, ws->M * 4 * 3)))) {
@@ -1238,15 +1255,15 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
             return cuda_status(e, "cudaFuncSetAttribute(k_g3adj)");
         }
     }
-    const char *xenv = std::getenv("PMX_XFAST");
-    ws->xfast = xpass_supported(ws->n0) && !(flags & PMX_WS_CUFFT3D) && !(xenv && xenv[0] == '0');
     size_t wk[4] = {0, 0, 0, 0};
     cufftHandle *ph[4];
     bool *hv[4];
-    const char *penv = std::getenv("PMX_PLANE");
-    ws->plane = ws->xfast && plane_supported(ws->n1, ws->n2) &&
-                ((flags & PMX_WS_PLANE) || (penv && penv[0] == '1')) && !(penv && penv[0] == '0');
     if (ws->plane) {
+        if ((st = plane_max_clusters(ws->n1, ws->n2, &ws->pcl)) ||
+            (st = alloc((void **)&ws->pscr, (size_t)ws->pcl * ws->n1 * ws->n2p * sizeof(float2)))) {
+            ws_free(ws);
+            return st;
+        }
         const int64_t np = 2 * ws->n1 + 1;
         std::vector<float2> ptw(np);
         plane_twiddles(ws->n1, ws->n2, ptw.data());

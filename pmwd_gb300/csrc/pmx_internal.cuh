@@ -76,18 +76,25 @@ int make_em_params(const pmx_enmesh_spec *spec, EmParams *p);
 // false): in = FFT_yz(rho) (n0, n1, n2h), out = the three gradient spectra
 // (n0, 3, n1, n2h) after the inverse x transform.  Adjoint: in = FFT_yz of
 // the three mesh cotangents (n0, 3, n1, n2h), out = (n0, n1, n2h).
+// Complex rows hold n2h values at a stride of rs >= n2h elements.
 bool xpass_supported(int64_t n0);
 int xpass(bool adj, const float2 *in, float2 *out, const float *kt, const float2 *tw, int64_t n0,
-          int64_t n1, int64_t n2h, float c, cudaStream_t st);
+          int64_t n1, int64_t n2h, int64_t rs, float c, cudaStream_t st);
+// n2h rounded up to a multiple of 4 complex values (32 bytes): the complex
+// row stride of the plane-kernel path, so every column tile of a plane
+// covers whole 32-byte sectors (HBM3e has no byte-masked writes).
+inline int64_t padded_row(int64_t n2h) { return (n2h + 3) & ~(int64_t)3; }
 void xpass_twiddles(int64_t n, float2 *host);
 
 // 2-D (y, z) transforms of consecutive planes (pmx_fft.cu): forward real
-// (n1, n2) -> complex (n1, n2/2+1), inverse complex -> real (input
-// destroyed); one thread-block cluster per plane.  ptw holds
-// plane_twiddles(n1, n2) (2 n1 + 1 entries for square planes).
+// (n1, n2) -> complex (n1, n2/2+1) at row stride padded_row(n2/2+1); inverse
+// complex -> real through a scratch plane per cluster (n1 * padded_row
+// complex values each, plane_max_clusters of them).  One thread-block cluster
+// per plane.  ptw holds plane_twiddles(n1, n2) (2 n1 + 1 entries).
 bool plane_supported(int64_t n1, int64_t n2);
+int plane_max_clusters(int64_t n1, int64_t n2, int *ncl);
 int plane_fft(bool inv, const void *in, void *out, const float2 *ptw, int64_t nplanes, int64_t n1,
-              int64_t n2, cudaStream_t st);
+              int64_t n2, float2 *scratch, int max_clusters, cudaStream_t st);
 void plane_twiddles(int64_t n1, int64_t n2, float2 *host);
 
 __device__ __forceinline__ int pymod(int x, int m) {
