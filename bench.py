@@ -414,13 +414,9 @@ def run_pmx(args, rank, world, local_rank):
                 'frac': ach / peak, 'traffic': tr,
                 'algorithmic_bytes': ab[dom], 'peak_kind': f'{peak_kind} (MEASURED_PEAKS.json hbm_gbs)'
                 if peak_kind == 'measured' else 'fallback 6.8 TB/s'}
-    # whole-step compulsory bytes: every stage's algorithmic bytes times its
-    # launches per step, plus the mesh fills (density twice, the three mesh
-    # cotangents once per fwd+adj step pair)
-    step_bytes = 4 * M * 2 + 12 * M
-    for name, (ms, calls) in stages.items():
-        if ab.get(name):
-            step_bytes += ab[name] * calls / args.steps
+    # whole-step compulsory bytes, the fixed convention of the hot-path
+    # survey: forward step 156 N + 64 M, adjoint step 336 N + 140 M
+    step_bytes = 492 * N + 204 * M
     step_gbs = step_bytes / (ms_step / 1e3) / 1e9
 
     cpu = None
@@ -441,8 +437,8 @@ def run_pmx(args, rank, world, local_rank):
         'roofline': roofline,
         'step_roofline': {'bytes_per_step': step_bytes, 'achieved': step_gbs, 'peak': peak,
                           'frac': step_gbs / peak, 'unit': 'GB/s',
-                          'convention': 'sum over stages of algorithmic bytes x launches, '
-                                        'plus 20 M bytes of mesh fills, per fwd+adj step pair'},
+                          'convention': '492 N + 204 M bytes per fwd+adj step pair '
+                                        '(forward 156 N + 64 M, adjoint 336 N + 140 M)'},
         'stages': stage_rows,
         'cpu_baseline': cpu,
         'e2e': e2e,
