@@ -238,6 +238,30 @@ int pmx_nbody_adj_step_kahan(pmx_workspace *ws, const pmx_enmesh_spec *spec,
                              double omega_m, double *dots, void *stream);
 
 /* --------------------------------------------------------------------------
+ * Power spectrum (pmwd/spec_util.py:50-147)
+ * ------------------------------------------------------------------------ */
+
+/* Bins the half spectra F (and G for a cross spectrum; NULL for auto) of a
+ * real grid of grid_shape: nbatch consecutive complex64 arrays of shape
+ * (n0, n1, n2/2+1) each, summed over the batch (the reference sums leading
+ * channel axes).  kx, ky, kz: float64 wavenumbers in cycles per sample
+ * (fftfreq, fftfreq, rfftfreq).  For every complex cell: k = |k|, bin =
+ * numpy.digitize(k, edges[0:nedges], right), kept when bin < nbin;
+ * multiplicity N = 1 on the z = 0 plane and (even n2) the z Nyquist plane,
+ * else 2; P = |F|^2 in float64, or F conj(G) in complex64 widened to
+ * float64 (re, im); times prod_axes sinc(k_axis)^-deconv when deconv != 0.
+ * Accumulates ksum[b] += k N, psum[2b], psum[2b+1] += P N, nsum[b] += N into
+ * caller-zeroed float64 device arrays.  ksum and nsum depend on the grid and
+ * bins only: for power-of-two grids up to 2048 both may be NULL (then only
+ * psum is accumulated, with float32 per-cell products and float64 sums).
+ * Replaces the digitize/bincount of spec_util.py:105-140. */
+int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
+                    const int64_t grid_shape[3], const double *kx,
+                    const double *ky, const double *kz, const double *edges,
+                    int32_t nedges, int32_t right, int32_t nbin, double deconv,
+                    double *ksum, double *psum, double *nsum, void *stream);
+
+/* --------------------------------------------------------------------------
  * Stage profiler (no counterpart in pmwd, which only times whole jitted
  * calls with timeit): CUDA events around each stage of the force and step
  * entry points of one workspace.

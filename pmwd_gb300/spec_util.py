@@ -52,6 +52,11 @@ def powspec(f, spacing, bins=1j / 3, g=None, deconv=None, cut_zero=True, cut_nyq
     bnum, bcut, edges, right = _getbins(grid_shape, bins, cut_nyq)
     dev = f.device
     F = fftfwd(f, axes=(-3, -2, -1))
+    if F.is_cuda and F.dtype == torch.complex64:
+        G = None if g is None else fftfwd(torch.as_tensor(g, device=dev), axes=(-3, -2, -1))
+        kk, PP, NN = _bin_cuda(F, G, grid_shape, edges, right, bnum, deconv)
+        return _finish(kk, PP, NN, edges.to(dev), bcut, cut_zero, spacing, grid_shape, dtype,
+                       g is not None)
     if g is None:
         P = F.real.to(dtype) ** 2 + F.imag.to(dtype) ** 2
     else:
@@ -78,8 +83,57 @@ def powspec(f, spacing, bins=1j / 3, g=None, deconv=None, cut_zero=True, cut_nyq
     kk = torch.zeros(bnum, dtype=dtype, device=dev).index_add_(0, b, (k * N).to(dtype))
     PP = torch.zeros(bnum, dtype=P.dtype, device=dev).index_add_(0, b, P * N.to(P.dtype))
     NN = torch.zeros(bnum, dtype=torch.float64, device=dev).index_add_(0, b, N)
+    return _finish(kk, PP, NN, e, bcut, cut_zero, spacing, grid_shape, dtype, g is not None)
+
+
+def _bin_cuda(F, G, grid_shape, edges, right, bnum, deconv):
+    """One pass of the pmx_powspec_bin kernel over the complex64 spectra:
+    per-bin sums of k N, P N and N in float64."""
+    from . import _lib
+    dev = F.device
+    nb = math.prod(F.shape[:-3])
+    F = F.contiguous()
+    if G is not None:
+        G = G.to(torch.complex64).contiguous()
+        if G.shape != F.shape:
+            raise ValueError(f'shape mismatch: {G.shape} != {F.shape}')
+    kx, ky, kz = (k.reshape(-1).contiguous() for k in
+                  fftfreq(grid_shape, None, dtype=torch.float64, device=dev))
+    e = edges.to(device=dev, dtype=torch.float64).contiguous()
+    psum = torch.zeros(bnum, 2, dtype=torch.float64, device=dev)
+    # the per-bin sums of k N and N depend on the grid and bins only: for
+    # power-of-two grids they are computed on the first call and reused
+    key = (dev, grid_shape, tuple(edges.tolist()), bool(right), bnum)
+    cached = _GEOMETRY.get(key) if _pow2_grid(grid_shape) else None
+    if cached is None:
+        ksum = torch.zeros(bnum, dtype=torch.float64, device=dev)
+        nsum = torch.zeros(bnum, dtype=torch.float64, device=dev)
+    else:
+        ksum = nsum = None
+    shape = (_lib.c_i64 * 3)(*grid_shape)
+    _lib.call('pmx_powspec_bin', torch.view_as_real(F), None if G is None else torch.view_as_real(G),
+              nb, shape, kx, ky, kz, e, len(e), int(right), bnum, float(deconv or 0.0), ksum, psum,
+              nsum, _lib.stream_ptr(dev))
+    if cached is None:
+        if _pow2_grid(grid_shape):
+            _GEOMETRY[key] = (ksum, nsum)
+    else:
+        ksum, nsum = cached[0].clone(), cached[1].clone()
+    PP = psum[:, 0] if G is None else torch.complex(psum[:, 0], psum[:, 1])
+    return ksum, PP, nsum
+
+
+_GEOMETRY = {}
+
+
+def _pow2_grid(grid_shape):
+    return all(s > 0 and s & (s - 1) == 0 for s in grid_shape) and max(grid_shape) <= 2048
+
+
+def _finish(kk, PP, NN, e, bcut, cut_zero, spacing, grid_shape, dtype, cross):
+    """Cut to [cut_zero, bcut) and normalise (spec_util.py:141-147)."""
     sl = slice(int(cut_zero), bcut)
     kk, PP, NN, edges = kk[sl], PP[sl], NN[sl], e[:bcut]
-    kk = kk / NN * 2 * math.pi / spacing
-    PP = PP / NN * spacing ** 3 / math.prod(grid_shape)
+    kk = kk.to(dtype) / NN * 2 * math.pi / spacing
+    PP = (PP if cross else PP.to(dtype)) / NN * spacing ** 3 / math.prod(grid_shape)
     return kk, PP, NN, edges * 2 * math.pi / spacing
