@@ -176,12 +176,14 @@ class _Job:
 
     # ---- one unit of device work per call ----
     def advance(self):
+        """Issues the job's next unit of work; returns False when it has to
+        wait (host setup or a device event still running)."""
         if self.phase == 'setup':
             if not self.setup_future.done():
-                return
+                return False
             self.setup_future.result()      # re-raises setup errors
             self.phase = 'fwd'
-            return
+            return True
         lib = _lib.load()
         P = _lib.ptr
         st = _lib.c_p(self.stream.cuda_stream)
@@ -236,10 +238,11 @@ class _Job:
             return
         if self.phase == 'adj_wait':
             if not self.event.query():
-                return
+                return False
             self._backprop()
             self._finish()
-            return
+            return True
+        return False  # done_wait
 
     def _backprop(self):
         """Chain the adjoint's results to the white-noise modes and Omega_m:
@@ -318,15 +321,22 @@ class Server:
                     if qi < len(pending):
                         time.sleep(max(0.0, min(0.002, pending[qi].arrival - now)))
                     continue
+                moved = False
                 for job in list(active):
-                    job.advance()
+                    if job.advance() is not False:
+                        moved = True
                     if job.ready():
+                        moved = True
                         res = job.result()
                         res.latency = (time.perf_counter() - t0) - job.t_arr
                         results[job.req.rid] = res
                         self.pool.release(job.ws)
                         used -= job.cost
                         active.remove(job)
+                if not moved:
+                    # every job waits on host setup or the device: yield the
+                    # GIL to the setup threads instead of spinning
+                    time.sleep(2e-4)
         finally:
             ex.shutdown(wait=True)
         torch.cuda.synchronize(self.dev)
