@@ -497,14 +497,18 @@ __device__ __forceinline__ void win_zero(float *buf, int nfloats) {
 
 // Forward: optional kick (vel += acc*K1) and drift (disp += vel*D), then the
 // CIC density deposit of the (new) positions.
-template <bool KD>
+// WIN: deposit through the warp windows; KAHAN: compensated updates (the
+// compensation arrays in h are then non-NULL).  Both are template arguments
+// so the default path carries neither their registers nor their branches.
+template <bool KD, bool WIN, bool KAHAN>
 __global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ pmid, float *disp,
                                             float *vel, const float *__restrict__ acc, int64_t n,
                                             float K1, float D, float *dens) {
     extern __shared__ __align__(16) float wsm[];
     const int lane = threadIdx.x & 31;
     float *buf = wsm + (threadIdx.x >> 5) * (WROWS * WZ);
-    if (h.win) win_zero(buf, WROWS * WZ);
+    float *const vcomp = KAHAN ? h.vcomp : nullptr, *const dcomp = KAHAN ? h.dcomp : nullptr;
+    if (WIN) win_zero(buf, WROWS * WZ);
     __syncwarp();
     // warp-uniform loop: each warp takes 32 consecutive particles
     for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); q0 < n;
@@ -515,14 +519,14 @@ __global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ p
         if (act) {
             float3 d = ld3(disp, q);
             if (KD) {
-                float3 v = kahan_axpy(ld3(vel, q), ld3(acc, q), K1, h.vcomp, q);
-                d = kahan_axpy(d, v, D, h.dcomp, q);
+                float3 v = kahan_axpy(ld3(vel, q), ld3(acc, q), K1, vcomp, q);
+                d = kahan_axpy(d, v, D, dcomp, q);
                 st3(vel, q, v);
                 st3(disp, q, d);
             }
             hot_enmesh(h, pmid, q, d, ax);
         }
-        if (!h.win) {
+        if (!WIN) {
             if (act) hot_deposit(h, ax, dens);
             continue;
         }
@@ -539,7 +543,7 @@ __global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ p
 }
 
 // Forward: gather the three acceleration meshes, optionally kick with K2.
-template <bool KICK>
+template <bool KICK, bool KAHAN>
 __global__ void __launch_bounds__(PT) k_gather3(Hot h, const int16_t *__restrict__ pmid,
                                                 const float *__restrict__ disp, float *vel,
                                                 float *acc, int64_t n, int64_t M,
@@ -560,14 +564,14 @@ __global__ void __launch_bounds__(PT) k_gather3(Hot h, const int16_t *__restrict
         }
         float3 a = make_float3(a0, a1, a2);
         st3(acc, q, a);
-        if (KICK) st3(vel, q, kahan_axpy(ld3(vel, q), a, K2, h.vcomp, q));
+        if (KICK) st3(vel, q, kahan_axpy(ld3(vel, q), a, K2, KAHAN ? h.vcomp : nullptr, q));
     }
 }
 
 // Adjoint: kick_adj(K1) then drift_adj(D) (nbody.py:80-99, 49-67), then the
 // density deposit of the reconstructed positions.  Partial dots:
 // slot 0 = sum(vel_cot*acc), slot 1 = sum(disp_cot*vel).
-template <bool KD>
+template <bool KD, bool WIN, bool KAHAN>
 __global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pmid, float *disp,
                                            float *vel, const float *__restrict__ acc,
                                            float *disp_cot, float *vel_cot,
@@ -577,7 +581,8 @@ __global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pm
     extern __shared__ __align__(16) float wsm[];
     const int lane = threadIdx.x & 31;
     float *buf = wsm + (threadIdx.x >> 5) * (WROWS * WZ);
-    if (h.win) win_zero(buf, WROWS * WZ);
+    float *const vcomp = KAHAN ? h.vcomp : nullptr, *const dcomp = KAHAN ? h.dcomp : nullptr;
+    if (WIN) win_zero(buf, WROWS * WZ);
     __syncwarp();
     double s0 = 0.0, s1 = 0.0;
     for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); q0 < n;
@@ -590,10 +595,10 @@ __global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pm
             if (KD) {
                 float3 a = ld3(acc, q);
                 float3 vc = ld3(vel_cot, q);
-                float3 v = kahan_axpy(ld3(vel, q), a, K1, h.vcomp, q);
+                float3 v = kahan_axpy(ld3(vel, q), a, K1, vcomp, q);
                 float3 dc = axmy3(ld3(disp_cot, q), ld3(alpha, q), K1);
                 s0 += dot3d(vc, a);
-                d = kahan_axpy(d, v, D, h.dcomp, q);
+                d = kahan_axpy(d, v, D, dcomp, q);
                 vc = axmy3(vc, dc, D);
                 s1 += dot3d(dc, v);
                 st3(vel, q, v);
@@ -603,7 +608,7 @@ __global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pm
             }
             hot_enmesh(h, pmid, q, d, ax);
         }
-        if (!h.win) {
+        if (!WIN) {
             if (act) hot_deposit(h, ax, dens);
             continue;
         }
@@ -631,6 +636,7 @@ __global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pm
 // disp_cot term sum_j vc_j sum_k g_j[k] dfrac_k / cell (into alpha), and the
 // gather VJP mesh term mcot_j[k] += vc_j frac_k.  Partial dot slot 2 =
 // sum(vel_cot * acc_new).
+template <bool WIN>
 __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__ pmid,
                                               const float *__restrict__ disp,
                                               const float *__restrict__ vel_cot, float *acc,
@@ -641,7 +647,7 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
     extern __shared__ __align__(16) float wsm[];
     const int lane = threadIdx.x & 31;
     float *buf = wsm + (threadIdx.x >> 5) * (3 * WROWS * WZ);
-    if (h.win) win_zero(buf, 3 * WROWS * WZ);
+    if (WIN) win_zero(buf, 3 * WROWS * WZ);
     __syncwarp();
     double s2 = 0.0;
     for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); q0 < n;
@@ -672,7 +678,7 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
                 c1 = __fadd_rn(c1, __fmul_rn(t, fg[1]));
                 c2 = __fadd_rn(c2, __fmul_rn(t, fg[2]));
             }
-            if (!h.win) {
+            if (!WIN) {
                 // gather-VJP mesh term mcot_j[k] += vc_j frac_k
 #pragma unroll
                 for (int p = 0; p < 4; ++p) {
@@ -692,7 +698,7 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
                                       __fdiv_rn(c2, h.cell)));
             s2 += dot3d(vc, a);
         }
-        if (!h.win) continue;
+        if (!WIN) continue;
         // gather-VJP mesh term through the warp window, three components
         const Win w = win_origin(act, ax);
         if (act) {
@@ -716,7 +722,7 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
 // Adjoint: scatter VJP disp_cot term sum_k (rho_cot[k] val) dfrac_k / cell
 // added into alpha, then optionally kick_adj(K2): vel += acc*K2,
 // disp_cot -= alpha*K2.
-template <bool KICK>
+template <bool KICK, bool KAHAN>
 __global__ void __launch_bounds__(PT) k_sadj(Hot h, const int16_t *__restrict__ pmid,
                                              const float *__restrict__ disp, float *vel,
                                              const float *__restrict__ acc, float *disp_cot,
@@ -743,7 +749,7 @@ __global__ void __launch_bounds__(PT) k_sadj(Hot h, const int16_t *__restrict__ 
                          __fadd_rn(al.z, __fdiv_rn(c2, h.cell)));
         st3(alpha, q, al);
         if (KICK) {
-            st3(vel, q, kahan_axpy(ld3(vel, q), ld3(acc, q), K2, h.vcomp, q));
+            st3(vel, q, kahan_axpy(ld3(vel, q), ld3(acc, q), K2, KAHAN ? h.vcomp : nullptr, q));
             st3(disp_cot, q, axmy3(ld3(disp_cot, q), al, K2));
         }
     }
@@ -861,6 +867,20 @@ int device_scratch(double **out) {
     *out = g_scratch[dev];
     return PMX_OK;
 }
+
+// Launches KERNEL<KD, WIN, KAHAN> for the Hot's window and compensation
+// settings (dynamic shared memory only with windows).
+#define PMX_WIN_LAUNCH(h, KERNEL, KD, grid, wsmem, st, args)                                   \
+    do {                                                                                       \
+        if ((h).win) {                                                                         \
+            if ((h).vcomp) KERNEL<PMX_UNPAREN KD, true, true><<<grid, PT, wsmem, st>>> args;   \
+            else KERNEL<PMX_UNPAREN KD, true, false><<<grid, PT, wsmem, st>>> args;            \
+        } else {                                                                               \
+            if ((h).vcomp) KERNEL<PMX_UNPAREN KD, false, true><<<grid, PT, 0, st>>> args;      \
+            else KERNEL<PMX_UNPAREN KD, false, false><<<grid, PT, 0, st>>> args;               \
+        }                                                                                      \
+    } while (0)
+#define PMX_UNPAREN(...) __VA_ARGS__
 
 int check_hot(pmx_workspace *ws, const pmx_enmesh_spec *spec, const void *pmid, const void *disp,
               int64_t n, int64_t ptcl_num, Hot *h) {
@@ -1248,7 +1268,7 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
     ws->win = (ws->n2 % 4 == 0) && ((flags & PMX_WS_WINDOW) || (wenv && wenv[0] == '1')) &&
               !(wenv && wenv[0] == '0');
     if (ws->win) {
-        cudaError_t e = cudaFuncSetAttribute(k_g3adj, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(k_g3adj<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)WIN3_SMEM);
         if (e != cudaSuccess) {
             ws_free(ws);
@@ -1379,8 +1399,9 @@ extern "C" int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec, const i
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
-            k_kds<false><<<stride_grid(n, PT), PT, WIN1_SMEM, s>>>(h, pmid, const_cast<float *>(disp), nullptr,
-                                                          nullptr, n, 0.f, 0.f, ws->dens);
+            PMX_WIN_LAUNCH(h, k_kds, (false), stride_grid(n, PT), WIN1_SMEM, s,
+                           (h, pmid, const_cast<float *>(disp), nullptr, nullptr, n, 0.f, 0.f,
+                            ws->dens));
             PMX_LAUNCH_CHECK("k_kds");
         }
     }
@@ -1388,8 +1409,8 @@ extern "C" int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec, const i
     if (n > 0) {
         {
             Stage sg(ws, 5, s, 1);
-            k_gather3<false><<<stride_grid(n, PT), PT, 0, s>>>(h, pmid, disp, nullptr, acc, n, ws->M,
-                                                              ws->g, 0.f);
+            k_gather3<false, false><<<stride_grid(n, PT), PT, 0, s>>>(h, pmid, disp, nullptr, acc, n,
+                                                                     ws->M, ws->g, 0.f);
             PMX_LAUNCH_CHECK("k_gather3");
         }
     }
@@ -1418,8 +1439,9 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
-            k_kds<false><<<G, PT, WIN1_SMEM, s>>>(h, pmid, const_cast<float *>(disp), nullptr, nullptr, n, 0.f,
-                                          0.f, ws->dens);
+            PMX_WIN_LAUNCH(h, k_kds, (false), G, WIN1_SMEM, s,
+                           (h, pmid, const_cast<float *>(disp), nullptr, nullptr, n, 0.f, 0.f,
+                            ws->dens));
             PMX_LAUNCH_CHECK("k_kds");
         }
     }
@@ -1427,8 +1449,12 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
     if (n > 0) {
         {
             Stage sg(ws, 7, s, 1);
-            k_g3adj<<<G, PT, h.win ? WIN3_SMEM : 0, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M, ws->g, ws->mcot,
-                                     ws->part);
+            if (h.win)
+                k_g3adj<true><<<G, PT, WIN3_SMEM, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M,
+                                                       ws->g, ws->mcot, ws->part);
+            else
+                k_g3adj<false><<<G, PT, 0, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M, ws->g,
+                                                ws->mcot, ws->part);
             PMX_LAUNCH_CHECK("k_g3adj");
         }
     }
@@ -1436,8 +1462,8 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
     if (n > 0) {
         {
             Stage sg(ws, 11, s, 1);
-            k_sadj<false><<<G, PT, 0, s>>>(h, pmid, disp, nullptr, nullptr, nullptr, disp_cot, n,
-                                           ws->dens, 0.f);
+            k_sadj<false, false><<<G, PT, 0, s>>>(h, pmid, disp, nullptr, nullptr, nullptr, disp_cot,
+                                                  n, ws->dens, 0.f);
             PMX_LAUNCH_CHECK("k_sadj");
         }
     }
@@ -1566,7 +1592,8 @@ static int nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int1
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
-            k_kds<true><<<G, PT, WIN1_SMEM, s>>>(h, pmid, disp, vel, acc, n, factors[0], factors[1], ws->dens);
+            PMX_WIN_LAUNCH(h, k_kds, (true), G, WIN1_SMEM, s,
+                           (h, pmid, disp, vel, acc, n, factors[0], factors[1], ws->dens));
             PMX_LAUNCH_CHECK("k_kds");
         }
     }
@@ -1574,7 +1601,12 @@ static int nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int1
     if (n > 0) {
         {
             Stage sg(ws, 5, s, 1);
-            k_gather3<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, ws->M, ws->g, factors[2]);
+            if (h.vcomp)
+                k_gather3<true, true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, ws->M, ws->g,
+                                                       factors[2]);
+            else
+                k_gather3<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, ws->M, ws->g,
+                                                        factors[2]);
             PMX_LAUNCH_CHECK("k_gather3");
         }
     }
@@ -1611,22 +1643,31 @@ static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const 
     if (G > PMAX) G = PMAX;
     {
         Stage sg(ws, 6, s, 1);
-        k_ka<true><<<G, PT, WIN1_SMEM, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n, factors[0],
-                                    factors[1], ws->dens, ws->part);
+        PMX_WIN_LAUNCH(h, k_ka, (true), G, WIN1_SMEM, s,
+                       (h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n, factors[0],
+                        factors[1], ws->dens, ws->part));
         PMX_LAUNCH_CHECK("k_ka");
     }
     if ((st = force_meshes(ws, h, omega_m, s))) return st;
     {
         Stage sg(ws, 7, s, 1);
-        k_g3adj<<<G, PT, h.win ? WIN3_SMEM : 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M, ws->g, ws->mcot,
-                                 ws->part);
+        if (h.win)
+            k_g3adj<true><<<G, PT, WIN3_SMEM, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M,
+                                                   ws->g, ws->mcot, ws->part);
+        else
+            k_g3adj<false><<<G, PT, 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M, ws->g,
+                                            ws->mcot, ws->part);
         PMX_LAUNCH_CHECK("k_g3adj");
     }
     if ((st = force_adj_meshes(ws, omega_m, s))) return st;
     {
         Stage sg(ws, 11, s, 1);
-        k_sadj<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n, ws->dens,
-                                      factors[2]);
+        if (h.vcomp)
+            k_sadj<true, true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n,
+                                                ws->dens, factors[2]);
+        else
+            k_sadj<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n,
+                                                 ws->dens, factors[2]);
         PMX_LAUNCH_CHECK("k_sadj");
     }
     {
