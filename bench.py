@@ -55,6 +55,9 @@ def parse():
     ap.add_argument('--serve', type=int, default=0,
                     help='serving mode: number of requests of the serving stream')
     ap.add_argument('--serve-sides', default='64,128,256')
+    ap.add_argument('--contention', action='store_true',
+                    help='scatter/gather contention stress: 256^3 particles, 256^3 mesh, 64 Mpc/h '
+                         'box evolved to a=1 vs the same particles on the lattice')
     ap.add_argument('--serve-steps', default='10,100')
     return ap.parse_args()
 
@@ -477,6 +480,92 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_contention(args):
+    """Scatter/gather contention stress (256^3 particles on a 256^3 mesh in a
+    64 Mpc/h box): one density scatter, one force and one 3-channel gather,
+    timed on the particles evolved to a = 1 (63 steps, halos with hundreds
+    of particles per cell) and on the same particles on the lattice."""
+    import numpy as np
+    import torch
+    import importlib
+    import pmwd_gb300 as pg
+    from pmwd_gb300 import _lib
+    gnb = importlib.import_module('pmwd_gb300.nbody')
+    torch.cuda.set_device(0)
+    dev = torch.device('cuda', 0)
+    lib = _lib.load()
+    side = 256
+    conf = pg.Configuration(0.25, (side,) * 3, 1)
+    cosmo = pg.boltzmann(pg.Cosmology(conf, **COSMO), conf)
+    N, M = conf.ptcl_num, conf.mesh_size
+    with torch.no_grad():
+        ptcl, _ = pg.lpt(pg.linear_modes(pg.white_noise(0, conf, device=dev), cosmo, conf),
+                         cosmo, conf)
+    pmid = ptcl.pmid.contiguous()
+    disp = ptcl.disp.detach().contiguous().clone()
+    vel = ptcl.vel.detach().contiguous().clone()
+    acc = torch.empty_like(disp)
+    ws = _lib.workspace(conf.mesh_shape, adjoint=True)
+    spec = _lib.make_spec(3, conf.mesh_shape, conf.mesh_shape, conf.cell_size)
+    P = _lib.ptr
+    stream = _lib.c_p(torch.cuda.current_stream(dev).cuda_stream)
+    Om = float(cosmo.Omega_m)
+    fwd = gnb.op_factors(gnb.forward_ops(conf), cosmo, conf).detach()
+    f_fwd = fwd.to(torch.float32).numpy().reshape(-1, 3)
+    _lib.check(lib.pmx_force(ws.handle, spec, P(pmid), P(disp), N, N, Om, P(acc), stream),
+               'pmx_force')
+    for i in range(f_fwd.shape[0]):
+        fac = (_lib.c_f * 3)(*f_fwd[i])
+        _lib.check(lib.pmx_nbody_step(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc), N, N, fac,
+                                      Om, stream), 'pmx_nbody_step')
+    torch.cuda.synchronize()
+    mesh = torch.zeros(conf.mesh_shape, dtype=torch.float32, device=dev)
+    mesh3 = torch.randn(conf.mesh_shape + (3,), dtype=torch.float32, device=dev)
+    out3 = torch.empty((N, 3), dtype=torch.float32, device=dev)
+    val = float(M / N)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    res = {}
+    for name, d in (('clustered', disp), ('lattice', torch.zeros_like(disp))):
+        def sc():
+            mesh.zero_()
+            _lib.check(lib.pmx_scatter(spec, P(pmid), P(d), N, None, val, 1, P(mesh), stream),
+                       'pmx_scatter')
+        def fo():
+            _lib.check(lib.pmx_force(ws.handle, spec, P(pmid), P(d), N, N, Om, P(acc), stream),
+                       'pmx_force')
+        def ga():
+            _lib.check(lib.pmx_gather(spec, P(pmid), P(d), N, P(mesh3), 3, None, 0.0, P(out3),
+                                      stream), 'pmx_gather')
+        t_zero = timed(lambda: mesh.zero_(), 10)
+        sc()
+        torch.cuda.synchronize()
+        peak = float(mesh.max()) / val  # particles (CIC weight) in the fullest cell
+        res[name] = {'scatter_ms': timed(sc, 10) - t_zero, 'force_ms': timed(fo, 5),
+                     'gather3_ms': timed(ga, 10), 'max_ptcl_per_cell': peak}
+        for k in ('scatter', 'gather3'):
+            res[name][k + '_ptcl_per_s'] = N / (res[name][k + '_ms'] / 1e3)
+    line = {'metric': 'scatter/gather contention (C3)', 'unit': 'ms',
+            'config': {'workload': f'{side}^3 ptcl / {side}^3 mesh, box 64 Mpc/h, evolved to a=1 '
+                                   f'in {f_fwd.shape[0]} steps vs the lattice',
+                       'ptcl': N, 'mesh_cells': M},
+            'clustered': res['clustered'], 'lattice': res['lattice'],
+            'clustered_over_lattice': {k: res['clustered'][k] / res['lattice'][k]
+                                       for k in ('scatter_ms', 'force_ms', 'gather3_ms')}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get('RANK', 0))
@@ -488,6 +577,10 @@ def main():
     if args.serve:
         if rank == 0:
             run_serve(args)
+        return
+    if args.contention:
+        if rank == 0:
+            run_contention(args)
         return
     if world > 1:
         import torch

@@ -9,6 +9,7 @@ import pytest
 import torch
 
 from oracle import cosmo as oc, ics, pm
+import pmwd_gb300 as pg
 from pmwd_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
@@ -164,6 +165,46 @@ def test_scatter_gather_and_vjps(cuda, case):
               T(vcot, cuda), _lib.ptr(dc), _lib.ptr(mc), _lib.stream_ptr(cuda))
     assert rel_l2(dc.cpu().numpy(), dc_o) < 1e-5
     assert rel_l2(mc.cpu().numpy(), mc_o) < RTOL_MESH
+
+
+def test_clustered_scatter_gather_force(cuda):
+    """Contention case (the C3 stress in miniature): 32^3 particles pulled into
+    8 halos of ~0.3-cell radius, up to ~10^3 particles per cell, so the
+    deposits' atomics collide.  Scatter, gather VJP (mesh atomics) and the
+    fused force path against the oracle."""
+    conf = oc.OConf(1.0, (32, 32, 32), 1, float_dtype=np.float32)
+    pmid, disp0 = ics.gen_grid(conf)
+    rng = np.random.default_rng(7)
+    centres = rng.uniform(0, 32, (8, 3))
+    which = rng.integers(0, 8, len(pmid))
+    target = centres[which] + rng.normal(0, 0.3, (len(pmid), 3))
+    disp = (target - pmid.astype(np.float64) * conf.cell_size).astype(np.float32)
+    n = len(pmid)
+    spec = _lib.make_spec(3, conf.mesh_shape, conf.mesh_shape, conf.cell_size)
+    dP, dD = T(pmid, cuda), T(disp, cuda)
+    vs = np.float32(conf.mesh_size / conf.ptcl_num)
+    ref = pm.scatter(pmid, disp, conf)
+    out = torch.zeros(conf.mesh_shape, dtype=torch.float32, device=cuda)
+    _lib.call('pmx_scatter', spec, dP, dD, n, None, float(vs), 1, out, _lib.stream_ptr(cuda))
+    assert float(ref.max()) / vs > 500       # the contention is real
+    assert rel_l2(out.cpu().numpy(), ref) < RTOL_MESH
+    mesh0 = rng.normal(size=conf.mesh_shape).astype(np.float32)
+    vcot = rng.normal(size=(n,)).astype(np.float32)
+    dc_o, mc_o, _ = pm.gather_vjp(pmid, disp, conf, mesh0, vcot)
+    dc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+    mc = torch.zeros(conf.mesh_shape, dtype=torch.float32, device=cuda)
+    _lib.call('pmx_gather_adj', spec, dP, dD, n, T(mesh0, cuda), 1, T(vcot, cuda), dc, mc,
+              _lib.stream_ptr(cuda))
+    assert rel_l2(dc.cpu().numpy(), dc_o) < 1e-5
+    assert rel_l2(mc.cpu().numpy(), mc_o) < RTOL_MESH
+    gconf = pg.Configuration(1.0, (32, 32, 32), 1)
+    acc_o = pm.gravity(pmid, disp, 0.3, conf)
+    for kw in ({}, {'cufft3d': True}):
+        ws = _lib.Workspace(gconf.mesh_shape, adjoint=True, **kw)
+        acc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+        _lib.call('pmx_force', ws.handle, spec, dP, dD, n, gconf.ptcl_num, 0.3, acc,
+                  _lib.stream_ptr(cuda))
+        assert rel_l2(acc.cpu().numpy(), acc_o) < 1e-5
 
 
 def test_scatter_centered_known_answer(cuda):
