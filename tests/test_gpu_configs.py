@@ -1,0 +1,96 @@
+"""The benchmark configurations that run on the GPU in seconds, at full size:
+
+* C1 -- plain forward run, float32: 64^3 particles on a 64^3 mesh, box
+  256 Mpc/h, A_s = 2.1e-9, n_s 0.965, Omega_m 0.3, Omega_b 0.05, h 0.7,
+  white noise from seed 0, 2LPT at a = 1/64, 63 leapfrog steps to a = 1.
+  Against the oracle from the same initial conditions: final position RMS
+  within 1e-3 of the particle spacing, and the matter power spectrum of the
+  CIC density within 0.1% below half the mesh Nyquist.
+* C2 -- forward plus reversible adjoint, float32: 128^3 particles on a 256^3
+  mesh, box 256 Mpc/h, 63 steps, objective sum of squared density contrast
+  at a = 1; gradients with respect to the white-noise modes and
+  (Omega_m, A_s) against central finite differences (relative step 1e-3).
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cosmo as oc, ics, nbody as onb, pm
+import pmwd_gb300 as pg
+
+pytestmark = pytest.mark.gpu
+
+COSMO = dict(A_s_1e9=2.1, n_s=0.965, Omega_m=0.3, Omega_b=0.05, h=0.7)
+
+
+def T(x, dev):
+    return torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+
+
+def test_c1_full_run_matches_oracle(cuda):
+    oconf = oc.OConf(4.0, (64, 64, 64), 1, float_dtype=np.float32)
+    gconf = pg.Configuration(4.0, (64, 64, 64), 1)
+    assert len(gconf.a_nbody) - 1 == 63
+    ocos = oc.with_tables(oc.OCosmo(**COSMO), oconf)
+    gcos = pg.boltzmann(pg.Cosmology(gconf, **COSMO), gconf)
+    noise = np.random.default_rng(0).standard_normal((64, 64, 64), dtype=np.float32)
+    pmid, disp, vel = ics.lpt(ics.linear_modes(noise, ocos, oconf), ocos, oconf)
+    st = onb.nbody(onb.State(pmid, disp, vel), ocos, oconf)
+    ptcl = pg.Particles(gconf, T(pmid, cuda), T(disp, cuda), vel=T(vel, cuda))
+    out, _ = pg.nbody(ptcl, None, gcos, gconf)
+    d_gpu = out.disp.cpu().numpy()
+    rms = np.sqrt(np.mean((d_gpu.astype(np.float64) - st.disp) ** 2))
+    assert rms < 1e-3 * oconf.ptcl_spacing, rms
+    # power spectra of the final CIC densities, below half the mesh Nyquist
+    k_o, P_o, _, _ = ics.powspec(pm.scatter(pmid, st.disp.astype(np.float32), oconf),
+                                 oconf.cell_size)
+    k_g, P_g, _, _ = ics.powspec(pm.scatter(pmid, d_gpu, oconf), oconf.cell_size)
+    knyq = np.pi / oconf.cell_size
+    sel = k_o < knyq / 2
+    assert sel.sum() > 5
+    err = np.abs(P_g[sel] / P_o[sel] - 1)
+    print(f'C1: position RMS {rms / oconf.ptcl_spacing:.2e} of the spacing, '
+          f'max |P/P_oracle - 1| {err.max():.2e} for k < k_Nyq/2')
+    assert err.max() < 1e-3, err.max()
+
+
+def c2_objective(modes, Om, As, conf):
+    c = dict(COSMO, Omega_m=Om, A_s_1e9=As)
+    cosmo = pg.boltzmann(pg.Cosmology(conf, **c), conf, varlin=False)
+    ptcl, _ = pg.lpt(pg.linear_modes(modes, cosmo, conf), cosmo, conf)
+    ptcl, _ = pg.nbody(ptcl, None, cosmo, conf)
+    dens = pg.scatter(ptcl, conf)
+    return (dens - 1).square().sum()
+
+
+def test_c2_gradients_vs_central_differences(cuda):
+    conf = pg.Configuration(2.0, (128, 128, 128), 2)
+    assert conf.mesh_shape == (256, 256, 256) and len(conf.a_nbody) - 1 == 63
+    modes = pg.white_noise(0, conf, real=True, device=cuda)
+    m = modes.clone().requires_grad_(True)
+    Om = torch.tensor(0.3, dtype=torch.float64, requires_grad=True)
+    As = torch.tensor(2.1, dtype=torch.float64, requires_grad=True)
+    c2_objective(m, Om, As, conf).backward()
+    g_m, g_Om, g_As = m.grad.clone(), float(Om.grad), float(As.grad)
+
+    def f(dm=None, om=0.3, a_s=2.1):
+        with torch.no_grad():
+            mm = modes if dm is None else modes + dm
+            return float(c2_objective(mm, torch.tensor(om, dtype=torch.float64),
+                                      torch.tensor(a_s, dtype=torch.float64), conf))
+
+    h = 1e-3 * 0.3
+    fd_om = (f(om=0.3 + h) - f(om=0.3 - h)) / (2 * h)
+    assert abs(g_Om / fd_om - 1) < 2e-2, ('Om', g_Om, fd_om)
+    h = 1e-3 * 2.1
+    fd_as = (f(a_s=2.1 + h) - f(a_s=2.1 - h)) / (2 * h)
+    assert abs(g_As / fd_as - 1) < 2e-2, ('As', g_As, fd_as)
+    u = torch.randn(modes.shape, device=cuda, generator=torch.Generator(device=cuda).manual_seed(1))
+    u = u / u.norm()
+    h = 1e-3 * float(modes.norm())
+    fd_u = (f(h * u) - f(-h * u)) / (2 * h)
+    ad = float((g_m * u).sum())
+    print(f'C2: adjoint / central difference - 1: Om {g_Om / fd_om - 1:.2e}, '
+          f'As {g_As / fd_as - 1:.2e}, modes {ad / fd_u - 1:.2e}')
+    assert abs(ad / fd_u - 1) < 2e-2, ('modes', ad, fd_u)
