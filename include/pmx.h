@@ -237,6 +237,29 @@ int pmx_nbody_adj_step_kahan(pmx_workspace *ws, const pmx_enmesh_spec *spec,
                              int64_t ptcl_num, const float factors[3],
                              double omega_m, double *dots, void *stream);
 
+/* nsteps consecutive forward steps (pmwd/nbody.py:193-223, default splits)
+ * in one call; factors (nsteps, 3) as pmx_nbody_step, host memory.  The
+ * gather + kick of step i and the kick + drift + deposit of step i+1 run as
+ * one particle pass with the same float32 updates in the same order, so the
+ * result equals nsteps calls of pmx_nbody_step up to the order of atomic
+ * adds. */
+int pmx_nbody_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                    const int16_t *pmid, float *disp, float *vel, float *acc,
+                    int64_t n, int64_t ptcl_num, int32_t nsteps,
+                    const float *factors, double omega_m, void *stream);
+
+/* nsteps consecutive reverse steps with the adjoint (pmwd/nbody.py:226-260)
+ * in one call; factors (nsteps, 3) as pmx_nbody_adj_step, host memory; dots
+ * (nsteps, 4) in DEVICE memory, row i as the dots of pmx_nbody_adj_step for
+ * step i.  The scatter VJP + kick_adj of step i and the kick_adj + drift_adj
+ * + deposit of step i+1 run as one particle pass. */
+int pmx_nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                        const int16_t *pmid, float *disp, float *vel,
+                        float *acc, float *disp_cot, float *vel_cot,
+                        float *acc_cot, int64_t n, int64_t ptcl_num,
+                        int32_t nsteps, const float *factors, double omega_m,
+                        double *dots, void *stream);
+
 /* --------------------------------------------------------------------------
  * Power spectrum (pmwd/spec_util.py:50-147)
  * ------------------------------------------------------------------------ */
@@ -267,7 +290,7 @@ int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
  * entry points of one workspace.
  * ------------------------------------------------------------------------ */
 
-#define PMX_PROF_STAGES 13
+#define PMX_PROF_STAGES 15
 
 /* Starts (on != 0) or stops recording stage events on this workspace. */
 int pmx_profile_enable(pmx_workspace *ws, int on);

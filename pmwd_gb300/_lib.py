@@ -61,6 +61,10 @@ SIGNATURES = {
     'pmx_nbody_adj_step_kahan': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_p, c_p, c_p, c_p, c_p,
                                          c_p, c_p, c_p, c_p, c_i64, c_i64, ctypes.POINTER(c_f),
                                          c_d, c_p, c_p]),
+    'pmx_nbody_steps': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_p, c_p, c_p, c_p, c_i64, c_i64,
+                                c_i32, c_p, c_d, c_p]),
+    'pmx_nbody_adj_steps': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_p, c_p, c_p, c_p, c_p, c_p,
+                                    c_p, c_i64, c_i64, c_i32, c_p, c_d, c_p, c_p]),
     'pmx_powspec_bin': (c_int, [c_p, c_p, c_i64, ctypes.POINTER(c_i64), c_p, c_p, c_p, c_p, c_i32,
                                 c_i32, c_i32, c_d, c_p, c_p, c_p, c_p]),
     'pmx_profile_enable': (c_int, [c_p, c_int]),
@@ -69,7 +73,7 @@ SIGNATURES = {
     'pmx_profile_stage_name': (ctypes.c_char_p, [c_int]),
 }
 
-PROF_STAGES = 13
+PROF_STAGES = 15
 
 
 def profile_read(ws):

@@ -113,6 +113,11 @@ struct pmx_workspace {
     bool graphs = false;        // slab loops captured as CUDA graphs
     cudaStream_t cap = nullptr, aux[KMAX] = {};
     cudaEvent_t fork = nullptr, join[KMAX] = {};
+    // the adjoint's density cotangent (rho_cot), in g behind the complex
+    // spectrum the last inverse transform reads: the density itself stays
+    // free, so a multi-step run can deposit the next step's density while
+    // it gathers rho_cot
+    float *rcot = nullptr;
     // stage profiler: CUDA events around every stage while enabled
     bool prof_on = false;
     struct Rec {
@@ -129,7 +134,7 @@ namespace {
 const char *const kStageNames[PMX_PROF_STAGES] = {
     "fill", "deposit_fwd", "r2c", "poisson_fwd", "c2r_x3", "gather3_kick",
     "kick_drift_adj_deposit", "gather3_adj", "r2c_x3", "poisson_adj", "c2r", "scatter_adj_kick",
-    "finish"};
+    "finish", "gather3_kick_kick_drift_deposit", "scatter_adj_kick_kick_drift_adj_deposit"};
 
 cudaEvent_t prof_event(pmx_workspace *ws) {
     if (!ws->pool.empty()) {
@@ -755,6 +760,104 @@ __global__ void __launch_bounds__(PT) k_sadj(Hot h, const int16_t *__restrict__ 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Kernels that join two consecutive steps of a multi-step run: the last
+// particle pass of step i and the first of step i+1 have no FFT between them,
+// so they run as one pass over the particles, with the same float32 updates
+// in the same order as the two kernels they replace (default path: no
+// windows, no compensation).
+// ---------------------------------------------------------------------------
+
+// k_gather3<true> of step i, then k_kds<true> of step i+1: gather, kick K2,
+// kick K1n, drift Dn, deposit.  acc is not stored: the next force rewrites it
+// before anything reads it.
+__global__ void __launch_bounds__(PT) k_gk_kds(Hot h, const int16_t *__restrict__ pmid, float *disp,
+                                               float *vel, int64_t n, const float *__restrict__ g,
+                                               float K2, float K1n, float Dn, float *dens) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        Axis ax[3];
+        float3 d = ld3(disp, q);
+        hot_enmesh(h, pmid, q, d, ax);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            int64_t c = hot_cell(h, ax, k);
+            float f = frac_of(ax, k);
+            const float *gc = g + c + (int64_t)ax[0].i[k & 1] * h.gxs;
+            a0 = __fadd_rn(a0, __fmul_rn(__ldg(gc), f));
+            a1 = __fadd_rn(a1, __fmul_rn(__ldg(gc + h.gjs), f));
+            a2 = __fadd_rn(a2, __fmul_rn(__ldg(gc + 2 * h.gjs), f));
+        }
+        const float3 a = make_float3(a0, a1, a2);
+        float3 v = axpy3(ld3(vel, q), a, K2);   // kick, step i
+        v = axpy3(v, a, K1n);                   // kick, step i+1
+        d = axpy3(d, v, Dn);                    // drift, step i+1
+        st3(vel, q, v);
+        st3(disp, q, d);
+        hot_enmesh(h, pmid, q, d, ax);
+        hot_deposit(h, ax, dens);
+    }
+}
+
+// k_sadj<true> of adjoint step i, then k_ka<true> of adjoint step i+1: the
+// scatter-VJP term into alpha, kick_adj K2, kick_adj K1n, drift_adj Dn,
+// deposit; partial dots of step i+1 into slots 0, 1.  alpha is not stored:
+// the next gather VJP rewrites it before anything reads it.
+__global__ void __launch_bounds__(PT) k_sa_ka(Hot h, const int16_t *__restrict__ pmid,
+                                              float *disp, float *vel,
+                                              const float *__restrict__ acc, float *disp_cot,
+                                              float *vel_cot, const float *__restrict__ alpha,
+                                              int64_t n, const float *__restrict__ rho_cot,
+                                              float K2, float K1n, float Dn, float *dens,
+                                              double *part) {
+    __shared__ double sh[PT / 32];
+    double s0 = 0.0, s1 = 0.0;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        Axis ax[3];
+        float3 d = ld3(disp, q);
+        hot_enmesh(h, pmid, q, d, ax);
+        float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            int64_t c = hot_cell(h, ax, k);
+            float fg[3];
+            frac_grad_of(ax, k, fg);
+            float t = __fmul_rn(__ldg(rho_cot + c), h.val);
+            c0 = __fadd_rn(c0, __fmul_rn(t, fg[0]));
+            c1 = __fadd_rn(c1, __fmul_rn(t, fg[1]));
+            c2 = __fadd_rn(c2, __fmul_rn(t, fg[2]));
+        }
+        float3 al = ld3(alpha, q);
+        al = make_float3(__fadd_rn(al.x, __fdiv_rn(c0, h.cell)),
+                         __fadd_rn(al.y, __fdiv_rn(c1, h.cell)),
+                         __fadd_rn(al.z, __fdiv_rn(c2, h.cell)));
+        const float3 a = ld3(acc, q);
+        float3 v = axpy3(ld3(vel, q), a, K2);            // kick_adj, step i
+        float3 dc = axmy3(ld3(disp_cot, q), al, K2);
+        float3 vc = ld3(vel_cot, q);
+        v = axpy3(v, a, K1n);                            // kick_adj, step i+1
+        dc = axmy3(dc, al, K1n);
+        s0 += dot3d(vc, a);
+        d = axpy3(d, v, Dn);                             // drift_adj, step i+1
+        vc = axmy3(vc, dc, Dn);
+        s1 += dot3d(dc, v);
+        st3(vel, q, v);
+        st3(disp, q, d);
+        st3(disp_cot, q, dc);
+        st3(vel_cot, q, vc);
+        hot_enmesh(h, pmid, q, d, ax);
+        hot_deposit(h, ax, dens);
+    }
+    double t0 = block_sum<PT>(s0, sh);
+    double t1 = block_sum<PT>(s1, sh);
+    if (threadIdx.x == 0) {
+        part[0 * PMAX + blockIdx.x] = t0;
+        part[1 * PMAX + blockIdx.x] = t1;
+    }
+}
+
 // Sums the per-block partials in a fixed order: dots[s] = sum of slot s for
 // s < nslots (dots may be NULL), and *om_out = om_scale * sum of slot 2
 // (om_out may be NULL).
@@ -1057,7 +1160,7 @@ int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t s
 }
 
 // The force VJP tail after k_g3adj has filled ws->mcot: r2c of the three
-// cotangent meshes, adjoint Fourier operator, c2r into ws->dens (then
+// cotangent meshes, adjoint Fourier operator, c2r into ws->rcot (then
 // rho_cot, scale folded in).
 int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
     float s = (float)(1.5 * (double)(float)omega_m);
@@ -1082,12 +1185,12 @@ int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
         }
         if (ws->plane) {
             Stage sg(ws, 10, st, 1);
-            int st2 = plane_fft(true, Sk, ws->dens, ws->ptw, ws->n0, ws->n1, ws->n2, ws->pscr,
+            int st2 = plane_fft(true, Sk, ws->rcot, ws->ptw, ws->n0, ws->n1, ws->n2, ws->pscr,
                                 ws->pcl, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 10, st, 0);
-            int st2 = slab_run(ws, 3, Sk, ws->dens, st);
+            int st2 = slab_run(ws, 3, Sk, ws->rcot, st);
             if (st2) return st2;
         }
         return PMX_OK;
@@ -1106,7 +1209,7 @@ int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
     {
         Stage sg(ws, 10, st, 0);
         PMX_CUFFT(cufftSetStream(ws->c2r1, st));
-        PMX_CUFFT(cufftExecC2R(ws->c2r1, reinterpret_cast<cufftComplex *>(ws->ck), ws->dens));
+        PMX_CUFFT(cufftExecC2R(ws->c2r1, reinterpret_cast<cufftComplex *>(ws->ck), ws->rcot));
     }
     return PMX_OK;
 }
@@ -1264,6 +1367,8 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
         ws_free(ws);
         return st;
     }
+    // rcot behind the complex spectrum held in g (2 n0 n1 n2p + M <= 3 M floats)
+    ws->rcot = ws->g + 2 * ws->n0 * ws->n1 * ws->n2p;
     const char *wenv = std::getenv("PMX_WIN");
     ws->win = (ws->n2 % 4 == 0) && ((flags & PMX_WS_WINDOW) || (wenv && wenv[0] == '1')) &&
               !(wenv && wenv[0] == '0');
@@ -1463,7 +1568,7 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
         {
             Stage sg(ws, 11, s, 1);
             k_sadj<false, false><<<G, PT, 0, s>>>(h, pmid, disp, nullptr, nullptr, nullptr, disp_cot,
-                                                  n, ws->dens, 0.f);
+                                                  n, ws->rcot, 0.f);
             PMX_LAUNCH_CHECK("k_sadj");
         }
     }
@@ -1664,10 +1769,10 @@ static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const 
         Stage sg(ws, 11, s, 1);
         if (h.vcomp)
             k_sadj<true, true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n,
-                                                ws->dens, factors[2]);
+                                                ws->rcot, factors[2]);
         else
             k_sadj<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n,
-                                                 ws->dens, factors[2]);
+                                                 ws->rcot, factors[2]);
         PMX_LAUNCH_CHECK("k_sadj");
     }
     {
@@ -1718,6 +1823,152 @@ extern "C" int pmx_nbody_adj_step_kahan(pmx_workspace *ws, const pmx_enmesh_spec
 // ---------------------------------------------------------------------------
 // stage profiler
 // ---------------------------------------------------------------------------
+
+// Multi-step runs: nsteps consecutive steps in one call, joining the last
+// particle pass of each step with the first of the next (k_gk_kds,
+// k_sa_ka).  With windows or compensation the steps run one by one.
+static int nbody_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int16_t *pmid,
+                       float *disp, float *vel, float *acc, int64_t n, int64_t ptcl_num,
+                       int32_t nsteps, const float *factors, double omega_m, void *stream) {
+    if (nsteps < 0 || (nsteps > 0 && !factors)) return fail(PMX_ERR_ARG, "bad nsteps/factors");
+    if (nsteps == 0) return PMX_OK;
+    Hot h;
+    int st = check_hot(ws, spec, pmid, disp, n, ptcl_num, &h);
+    if (st) return st;
+    if (n > 0 && (!vel || !acc)) return fail(PMX_ERR_ARG, "null vel/acc");
+    if (h.win || n == 0) {
+        for (int32_t i = 0; i < nsteps; ++i)
+            if ((st = nbody_step(ws, spec, pmid, disp, vel, acc, n, ptcl_num, factors + 3 * i,
+                                 omega_m, nullptr, nullptr, stream)))
+                return st;
+        return PMX_OK;
+    }
+    cudaStream_t s = as_stream(stream);
+    if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
+    const int G = stride_grid(n, PT);
+    {
+        Stage sg(ws, 0, s, 1);
+        k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
+        PMX_LAUNCH_CHECK("k_fill");
+    }
+    {
+        Stage sg(ws, 1, s, 1);
+        k_kds<true, false, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, factors[0],
+                                                     factors[1], ws->dens);
+        PMX_LAUNCH_CHECK("k_kds");
+    }
+    for (int32_t i = 0; i < nsteps; ++i) {
+        const float *f = factors + 3 * i;
+        if ((st = force_meshes(ws, h, omega_m, s))) return st;
+        if (i + 1 < nsteps) {
+            {
+                Stage sg(ws, 0, s, 1);
+                k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
+                PMX_LAUNCH_CHECK("k_fill");
+            }
+            Stage sg(ws, 13, s, 1);
+            k_gk_kds<<<G, PT, 0, s>>>(h, pmid, disp, vel, n, ws->g, f[2], f[3], f[4], ws->dens);
+            PMX_LAUNCH_CHECK("k_gk_kds");
+        } else {
+            Stage sg(ws, 5, s, 1);
+            k_gather3<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, ws->M, ws->g, f[2]);
+            PMX_LAUNCH_CHECK("k_gather3");
+        }
+    }
+    return PMX_OK;
+}
+
+static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int16_t *pmid,
+                           float *disp, float *vel, float *acc, float *disp_cot, float *vel_cot,
+                           float *acc_cot, int64_t n, int64_t ptcl_num, int32_t nsteps,
+                           const float *factors, double omega_m, double *dots, void *stream) {
+    if (nsteps < 0 || (nsteps > 0 && (!factors || !dots)))
+        return fail(PMX_ERR_ARG, "bad nsteps/factors/dots");
+    if (nsteps == 0) return PMX_OK;
+    Hot h;
+    int st = check_hot(ws, spec, pmid, disp, n, ptcl_num, &h);
+    if (st) return st;
+    if (!(ws->flags & PMX_WS_ADJOINT)) return fail(PMX_ERR_ARG, "workspace lacks PMX_WS_ADJOINT");
+    if (n > 0 && (!vel || !acc || !disp_cot || !vel_cot || !acc_cot))
+        return fail(PMX_ERR_ARG, "null particle array");
+    if (h.win || n == 0) {
+        for (int32_t i = 0; i < nsteps; ++i)
+            if ((st = nbody_adj_step(ws, spec, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n,
+                                     ptcl_num, factors + 3 * i, omega_m, dots + 4 * i, nullptr,
+                                     nullptr, stream)))
+                return st;
+        return PMX_OK;
+    }
+    cudaStream_t s = as_stream(stream);
+    if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
+    int G = stride_grid(n, PT);
+    if (G > PMAX) G = PMAX;
+    {
+        Stage sg(ws, 0, s, 2);
+        k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
+        k_fill<<<grid_fill(3 * ws->M), 256, 0, s>>>(ws->mcot, 0.f, 3 * ws->M);
+        PMX_LAUNCH_CHECK("k_fill");
+    }
+    {
+        Stage sg(ws, 6, s, 1);
+        k_ka<true, false, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot,
+                                                    acc_cot, n, factors[0], factors[1], ws->dens,
+                                                    ws->part);
+        PMX_LAUNCH_CHECK("k_ka");
+    }
+    for (int32_t i = 0; i < nsteps; ++i) {
+        const float *f = factors + 3 * i;
+        if ((st = force_meshes(ws, h, omega_m, s))) return st;
+        {
+            Stage sg(ws, 7, s, 1);
+            k_g3adj<false><<<G, PT, 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M, ws->g,
+                                            ws->mcot, ws->part);
+            PMX_LAUNCH_CHECK("k_g3adj");
+        }
+        {
+            Stage sg(ws, 12, s, 1);
+            k_finish<<<1, 1024, 0, s>>>(ws->part, G, dots + 4 * i, 3, dots + 4 * i + 3,
+                                        om_scale(omega_m));
+            PMX_LAUNCH_CHECK("k_finish");
+        }
+        if ((st = force_adj_meshes(ws, omega_m, s))) return st;
+        if (i + 1 < nsteps) {
+            {
+                Stage sg(ws, 0, s, 2);
+                k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
+                k_fill<<<grid_fill(3 * ws->M), 256, 0, s>>>(ws->mcot, 0.f, 3 * ws->M);
+                PMX_LAUNCH_CHECK("k_fill");
+            }
+            Stage sg(ws, 14, s, 1);
+            k_sa_ka<<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n,
+                                     ws->rcot, f[2], f[3], f[4], ws->dens, ws->part);
+            PMX_LAUNCH_CHECK("k_sa_ka");
+        } else {
+            Stage sg(ws, 11, s, 1);
+            k_sadj<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n,
+                                                 ws->rcot, f[2]);
+            PMX_LAUNCH_CHECK("k_sadj");
+        }
+    }
+    return PMX_OK;
+}
+
+extern "C" int pmx_nbody_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                               const int16_t *pmid, float *disp, float *vel, float *acc,
+                               int64_t n, int64_t ptcl_num, int32_t nsteps, const float *factors,
+                               double omega_m, void *stream) {
+    return nbody_steps(ws, spec, pmid, disp, vel, acc, n, ptcl_num, nsteps, factors, omega_m,
+                       stream);
+}
+
+extern "C" int pmx_nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                                   const int16_t *pmid, float *disp, float *vel, float *acc,
+                                   float *disp_cot, float *vel_cot, float *acc_cot, int64_t n,
+                                   int64_t ptcl_num, int32_t nsteps, const float *factors,
+                                   double omega_m, double *dots, void *stream) {
+    return nbody_adj_steps(ws, spec, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n,
+                           ptcl_num, nsteps, factors, omega_m, dots, stream);
+}
 
 extern "C" int pmx_profile_enable(pmx_workspace *ws, int on) {
     if (!ws) return fail(PMX_ERR_ARG, "null workspace");

@@ -20,6 +20,9 @@ d(objective)/d(factor) = -dot for every adjoint factor (the reference's
 and torch autograd chains them through the factor functions.
 """
 
+import ctypes
+
+import numpy as np
 import torch
 
 from . import _lib
@@ -154,17 +157,20 @@ def run_forward(pmid, disp, vel, acc, ops, factors32, Om, conf, ws=None):
         _lib.check(lib.pmx_force(ws.handle, spec, P(pmid), P(disp), n, conf.ptcl_num, Om, P(acc),
                                  st), 'pmx_force')
         f = factors32.reshape(-1, 3)
-        if conf.kahan:
-            dcomp, vcomp = torch.zeros_like(disp), torch.zeros_like(vel)
+        if not conf.kahan:
+            # all steps in one call: consecutive steps share a particle pass
+            fac = np.ascontiguousarray(f, dtype=np.float32)
+            _lib.check(lib.pmx_nbody_steps(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc), n,
+                                           conf.ptcl_num, f.shape[0],
+                                           fac.ctypes.data_as(ctypes.c_void_p), Om, st),
+                       'pmx_nbody_steps')
+            return
+        dcomp, vcomp = torch.zeros_like(disp), torch.zeros_like(vel)
         for i in range(f.shape[0]):
             fac = (_lib.c_f * 3)(*f[i])
-            if conf.kahan:
-                _lib.check(lib.pmx_nbody_step_kahan(ws.handle, spec, P(pmid), P(disp), P(vel),
-                                                    P(acc), P(dcomp), P(vcomp), n, conf.ptcl_num,
-                                                    fac, Om, st), 'pmx_nbody_step_kahan')
-            else:
-                _lib.check(lib.pmx_nbody_step(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc),
-                                              n, conf.ptcl_num, fac, Om, st), 'pmx_nbody_step')
+            _lib.check(lib.pmx_nbody_step_kahan(ws.handle, spec, P(pmid), P(disp), P(vel),
+                                                P(acc), P(dcomp), P(vcomp), n, conf.ptcl_num,
+                                                fac, Om, st), 'pmx_nbody_step_kahan')
         return
     j = 0
     for o in ops:
@@ -200,20 +206,21 @@ def run_adjoint(pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, ops, factors32
                                      P(vel_cot), P(acc), P(acc_cot), P(dd[nsteps, 3:]), st),
                    'pmx_force_vjp')
         f = factors32.reshape(-1, 3)
-        if conf.kahan:
+        if not conf.kahan:
+            fac = np.ascontiguousarray(f, dtype=np.float32)
+            _lib.check(lib.pmx_nbody_adj_steps(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc),
+                                               P(disp_cot), P(vel_cot), P(acc_cot), n,
+                                               conf.ptcl_num, nsteps,
+                                               fac.ctypes.data_as(ctypes.c_void_p), Om, P(dd),
+                                               st), 'pmx_nbody_adj_steps')
+        else:
             dcomp, vcomp = torch.zeros_like(disp), torch.zeros_like(vel)
-        for i in range(nsteps):
-            fac = (_lib.c_f * 3)(*f[i])
-            if conf.kahan:
+            for i in range(nsteps):
+                fac = (_lib.c_f * 3)(*f[i])
                 _lib.check(lib.pmx_nbody_adj_step_kahan(
                     ws.handle, spec, P(pmid), P(disp), P(vel), P(acc), P(disp_cot), P(vel_cot),
                     P(acc_cot), P(dcomp), P(vcomp), n, conf.ptcl_num, fac, Om, P(dd[i]), st),
                     'pmx_nbody_adj_step_kahan')
-            else:
-                _lib.check(lib.pmx_nbody_adj_step(ws.handle, spec, P(pmid), P(disp), P(vel),
-                                                  P(acc), P(disp_cot), P(vel_cot), P(acc_cot), n,
-                                                  conf.ptcl_num, fac, Om, P(dd[i]), st),
-                           'pmx_nbody_adj_step')
         dd = dd.cpu()
         # factor order per step: K1_adj (dot0), D_adj (dot1), K2_adj (dot2)
         dots = dd[:nsteps, :3].reshape(-1)

@@ -209,6 +209,55 @@ def test_fused_step_equals_generic_ops(cuda, nb_case):
     assert rel_l2(generic.vel.cpu().numpy(), fused.vel.cpu().numpy()) < 1e-5
 
 
+def test_multistep_equals_single_steps(cuda, nb_case):
+    """pmx_nbody_steps / pmx_nbody_adj_steps (consecutive steps joined in one
+    particle pass) against the same steps called one by one: the float32
+    updates are the same, only the order of the atomic adds differs (the
+    forward state to 1e-5 after 8 steps, the adjoint's outputs, which
+    amplify it, to 1e-4)."""
+    import ctypes
+    oconf, gconf, pmid, disp, vel, ocos, gcos = nb_case
+    fwd = gnb.op_factors(gnb.forward_ops(gconf), gcos, gconf).detach()
+    adj = gnb.op_factors(gnb.adjoint_ops(gconf), gcos, gconf).detach()
+    f_fwd = np.ascontiguousarray(fwd.to(torch.float32).numpy().reshape(-1, 3))
+    f_adj = np.ascontiguousarray(adj.to(torch.float32).numpy().reshape(-1, 3))
+    nst = f_fwd.shape[0]
+    n = len(pmid)
+    spec = _lib.make_spec(3, gconf.mesh_shape, gconf.mesh_shape, gconf.cell_size)
+    st = _lib.stream_ptr(cuda)
+    Om = float(gcos.Omega_m)
+    out = []
+    for multi in (False, True):
+        ws = _lib.Workspace(gconf.mesh_shape, adjoint=True)
+        P_, D, V = T(pmid, cuda), T(disp, cuda), T(vel, cuda)
+        A = torch.empty_like(D)
+        rng = np.random.default_rng(2)
+        dc, vc = T(rng.normal(size=disp.shape).astype(np.float32), cuda), torch.zeros_like(D)
+        al = torch.zeros_like(D)
+        dots = torch.zeros((nst, 4), dtype=torch.float64, device=cuda)
+        _lib.call('pmx_force', ws.handle, spec, P_, D, n, gconf.ptcl_num, Om, A, st)
+        if multi:
+            _lib.call('pmx_nbody_steps', ws.handle, spec, P_, D, V, A, n, gconf.ptcl_num, nst,
+                      f_fwd.ctypes.data_as(ctypes.c_void_p), Om, st)
+            fwd_state = [t.cpu().numpy() for t in (D, V, A)]
+            _lib.call('pmx_nbody_adj_steps', ws.handle, spec, P_, D, V, A, dc, vc, al, n,
+                      gconf.ptcl_num, nst, f_adj.ctypes.data_as(ctypes.c_void_p), Om, dots, st)
+        else:
+            for i in range(nst):
+                _lib.call('pmx_nbody_step', ws.handle, spec, P_, D, V, A, n, gconf.ptcl_num,
+                          (_lib.c_f * 3)(*f_fwd[i]), Om, st)
+            fwd_state = [t.cpu().numpy() for t in (D, V, A)]
+            for i in range(nst):
+                _lib.call('pmx_nbody_adj_step', ws.handle, spec, P_, D, V, A, dc, vc, al, n,
+                          gconf.ptcl_num, (_lib.c_f * 3)(*f_adj[i]), Om, dots[i], st)
+        out.append((fwd_state, [t.cpu().numpy() for t in (D, V, A, dc, vc, dots)]))
+        del ws
+    for a, b in zip(out[0][0], out[1][0]):
+        assert rel_l2(b, a) < 1e-5
+    for a, b in zip(out[0][1], out[1][1]):
+        assert rel_l2(b, a) < 1e-4
+
+
 def test_factors_match_oracle(nb_case):
     oconf, gconf, pmid, disp, vel, ocos, gcos = nb_case
     ops = gnb.forward_ops(gconf)
