@@ -17,6 +17,7 @@ shard); value = total particle-steps of all ranks / max-over-ranks time.
 """
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -84,11 +85,16 @@ def algorithmic_bytes(N, M, Mc):
         'c2r': 8 * Mc + 4 * M,
         'scatter_adj_kick': 6 * N + 12 * N + 4 * M + 24 * N + 24 * N + 12 * N + 24 * N,
         'finish': None,
+        # consecutive steps joined: gather + kick, kick + drift + deposit
+        'gather3_kick_kick_drift_deposit': 6 * N + 48 * N + 12 * M + 4 * M,
+        # scatter VJP + kick_adj, kick_adj + drift_adj + deposit
+        'scatter_adj_kick_kick_drift_adj_deposit': 6 * N + 120 * N + 4 * M + 4 * M,
     }
 
 
 OWN_KERNELS = ('deposit_fwd', 'poisson_fwd', 'gather3_kick', 'kick_drift_adj_deposit',
-               'gather3_adj', 'poisson_adj', 'scatter_adj_kick')
+               'gather3_adj', 'poisson_adj', 'scatter_adj_kick', 'gather3_kick_kick_drift_deposit',
+               'scatter_adj_kick_kick_drift_adj_deposit')
 
 
 class ClockSampler:
@@ -239,7 +245,8 @@ def workload_config(args, world):
     side = args.ptcl
     mside = int(round(side * args.mesh))
     return {'workload': f'{side}^3 ptcl / {mside}^3 mesh, box {side * args.spacing:g} Mpc/h, '
-                        f'1 fwd + 1 adjoint leapfrog step of a {args.nbody_steps}-step run',
+                        f'K forward leapfrog steps then their K reversible-adjoint steps of a '
+                        f'{args.nbody_steps}-step run (rates per fwd+adj step pair)',
             'ptcl': side ** 3, 'mesh_cells': mside ** 3, 'parallelism': f'replicas x{world}',
             'l2': 'inputs larger than L2 (mesh 4.3 GB per array)'}
 
@@ -311,17 +318,37 @@ def run_pmx(args, rank, world, local_rank):
     alpha = torch.zeros_like(disp)
     torch.cuda.empty_cache()
 
-    # factors of the first step and of its adjoint (float64 -> float32)
+    # factors of the run (float64 -> float32): the timed segment is its first
+    # K forward steps, then the adjoint of those K steps (the last K rows of
+    # the reverse-time adjoint table), as a run executes them
     fwd = gnb.op_factors(gnb.forward_ops(conf), cosmo, conf).detach()
     adj = gnb.op_factors(gnb.adjoint_ops(conf), cosmo, conf).detach()
-    f_fwd = (_lib.c_f * 3)(*fwd[:3].to(torch.float32).tolist())
-    f_adj = (_lib.c_f * 3)(*adj[-3:].to(torch.float32).tolist())
+    fwd32 = np.ascontiguousarray(fwd.to(torch.float32).numpy().reshape(-1, 3))
+    adj32 = np.ascontiguousarray(adj.to(torch.float32).numpy().reshape(-1, 3))
+    f_fwd = (_lib.c_f * 3)(*fwd32[0])
+    f_adj = (_lib.c_f * 3)(*adj32[-1])
     Om = float(cosmo.Omega_m)
 
     ws = _lib.workspace(conf.mesh_shape, adjoint=True)
     spec = _lib.make_spec(3, conf.mesh_shape, conf.mesh_shape, conf.cell_size)
     dots = torch.zeros(4, dtype=torch.float64, device=dev)
     P = _lib.ptr
+    if max(args.steps, args.warmup) > fwd32.shape[0]:
+        raise SystemExit(f'--steps/--warmup exceed the {fwd32.shape[0]}-step run')
+    seg_dots = torch.zeros((fwd32.shape[0], 4), dtype=torch.float64, device=dev)
+
+    def segment(stream, k):
+        """The run's first k forward steps, then their k adjoint steps
+        (multi-step calls: consecutive steps share particle passes)."""
+        sf = np.ascontiguousarray(fwd32[:k])
+        sa = np.ascontiguousarray(adj32[-k:])
+        _lib.check(lib.pmx_nbody_steps(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc), N, N,
+                                       k, sf.ctypes.data_as(ctypes.c_void_p), Om, stream),
+                   'pmx_nbody_steps')
+        _lib.check(lib.pmx_nbody_adj_steps(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc),
+                                           P(disp_cot), P(vel_cot), P(alpha), N, N, k,
+                                           sa.ctypes.data_as(ctypes.c_void_p), Om,
+                                           P(seg_dots), stream), 'pmx_nbody_adj_steps')
 
     def step(stream):
         _lib.check(lib.pmx_nbody_step(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc), N, N,
@@ -333,8 +360,8 @@ def run_pmx(args, rank, world, local_rank):
     stream = torch.cuda.current_stream(dev)
     sp = _lib.c_p(stream.cuda_stream)
     _lib.check(lib.pmx_force(ws.handle, spec, P(pmid), P(disp), N, N, Om, P(acc), sp), 'force')
-    for _ in range(args.warmup):
-        step(sp)
+    segment(sp, args.warmup)
+    step(sp)                       # the single-step entry points used by e2e
     torch.cuda.synchronize()
     _lib.profile_read(ws)  # clear counters
 
@@ -351,8 +378,7 @@ def run_pmx(args, rank, world, local_rank):
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     torch.cuda.nvtx.range_push('timed')   # lets ncu --nvtx-include timed/ select these launches
-    for _ in range(args.steps):
-        step(sp)
+    segment(sp, args.steps)
     torch.cuda.nvtx.range_pop()
     e1.record(stream)
     barrier()
