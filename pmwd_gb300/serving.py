@@ -11,10 +11,10 @@ The server
 * prepares each admitted request (float64 background tables, white noise,
   2LPT) on a host worker thread, so host work overlaps device work;
 * runs every simulation as a job on its own CUDA stream and advances the
-  jobs in turn one leapfrog step (forward or adjoint) at a time, so kernels
-  of different simulations overlap on the device and a newly admitted
-  request starts while others are mid-run (continuous batching at step
-  granularity);
+  jobs in turn a few leapfrog steps (forward or adjoint; one multi-step call
+  of up to STEP_CHUNK steps) at a time, so kernels of different simulations
+  overlap on the device and a newly admitted request starts while others
+  are mid-run (continuous batching at step granularity);
 * retires a job when the event after its last work completes, frees its
   slot and memory, and admits waiting requests;
 * records per-request latency (arrival -> result ready): sims/s, p50, p99.
@@ -24,6 +24,7 @@ own stream), so a result is the same alone and in the mix up to the order
 of float32 atomic adds.
 """
 
+import ctypes
 import importlib
 import threading
 import time
@@ -43,6 +44,10 @@ from .particles import Particles
 from .scatter import scatter
 
 _nb = importlib.import_module('pmwd_gb300.nbody')
+
+# leapfrog steps a job issues per scheduling turn (one multi-step call, in
+# which consecutive steps share particle passes)
+STEP_CHUNK = 8
 
 
 @dataclass
@@ -190,11 +195,13 @@ class _Job:
         n = self.pmid.shape[0]
         conf = self.conf
         if self.phase == 'fwd':
-            fac = (_lib.c_f * 3)(*self.f_fwd[self.i])
-            _lib.check(lib.pmx_nbody_step(self.ws.handle, self.spec, P(self.pmid), P(self.disp),
-                                          P(self.vel), P(self.acc), n, conf.ptcl_num, fac,
-                                          self.Om, st), 'pmx_nbody_step')
-            self.i += 1
+            k = min(STEP_CHUNK, self.f_fwd.shape[0] - self.i)
+            fac = np.ascontiguousarray(self.f_fwd[self.i:self.i + k])
+            _lib.check(lib.pmx_nbody_steps(self.ws.handle, self.spec, P(self.pmid), P(self.disp),
+                                           P(self.vel), P(self.acc), n, conf.ptcl_num, k,
+                                           fac.ctypes.data_as(ctypes.c_void_p), self.Om, st),
+                       'pmx_nbody_steps')
+            self.i += k
             if self.i == self.f_fwd.shape[0]:
                 self.phase = 'objective'
             return
@@ -221,13 +228,15 @@ class _Job:
             self.i = 0
             return
         if self.phase == 'adj':
-            fac = (_lib.c_f * 3)(*self.f_adj[self.i])
-            _lib.check(lib.pmx_nbody_adj_step(self.ws.handle, self.spec, P(self.pmid),
-                                              P(self.disp), P(self.vel), P(self.acc),
-                                              P(self.disp_cot), P(self.vel_cot), P(self.alpha),
-                                              n, conf.ptcl_num, fac, self.Om, P(self.dd[self.i]),
-                                              st), 'pmx_nbody_adj_step')
-            self.i += 1
+            k = min(STEP_CHUNK, self.f_adj.shape[0] - self.i)
+            fac = np.ascontiguousarray(self.f_adj[self.i:self.i + k])
+            _lib.check(lib.pmx_nbody_adj_steps(self.ws.handle, self.spec, P(self.pmid),
+                                               P(self.disp), P(self.vel), P(self.acc),
+                                               P(self.disp_cot), P(self.vel_cot), P(self.alpha),
+                                               n, conf.ptcl_num, k,
+                                               fac.ctypes.data_as(ctypes.c_void_p), self.Om,
+                                               P(self.dd[self.i]), st), 'pmx_nbody_adj_steps')
+            self.i += k
             if self.i == self.f_adj.shape[0]:
                 self.host_dd = torch.empty(self.dd.shape, dtype=torch.float64, pin_memory=True)
                 with torch.cuda.stream(self.stream):
