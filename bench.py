@@ -1,12 +1,15 @@
 #!/usr/bin/env python
 """Throughput of pmwd's particle-mesh hot path on GB300.
 
-One bench step = one forward leapfrog step (K/2 D F K/2, nbody.py:121-140)
-plus one reversible-adjoint step (kick_adj, drift_adj, force_adj, kick_adj,
-nbody.py:143-162) of the 512^3-particle / 1024^3-mesh simulation (box
-1024 Mpc/h, 2LPT initial conditions at a = 1/64, 100 steps to a = 1),
-starting from the 2LPT state.  The metric is particle-steps per second of
-forward + adjoint (N particles per step pair).
+The timed region is a segment of the 512^3-particle / 1024^3-mesh run (box
+1024 Mpc/h, 2LPT initial conditions at a = 1/64, 100 steps to a = 1): its
+first K forward leapfrog steps (K/2 D F K/2, nbody.py:121-140) through one
+multi-step call, then the K reversible-adjoint steps of those (kick_adj,
+drift_adj, force_adj, kick_adj, nbody.py:143-162) through another.  One
+bench step is one forward + adjoint step pair; the metric is particle-steps
+per second of forward + adjoint (N particles per step pair).  The e2e figure
+runs single step pairs through the C ABI with every input copied in from
+pinned host memory and every output copied back.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl pmx|reference]
 
@@ -406,14 +409,31 @@ def run_pmx(args, rank, world, local_rank):
         outs = ('disp', 'vel', 'acc', 'disp_cot', 'vel_cot', 'alpha')
         d2h = sum(host[k].numel() * host[k].element_size() for k in outs)
         ke = max(2, min(args.steps, 5))
+        # one copy stream per buffer: copies of different buffers overlap,
+        # and a buffer's read-back overlaps other buffers' uploads; each
+        # buffer's copies stay in order on its own stream
+        cstreams = {k: torch.cuda.Stream(dev) for k in host}
         barrier()
         e0.record(stream)
+        done = None
         for _ in range(ke):
             for k, v in host.items():
-                dev_bufs[k].copy_(v, non_blocking=True)
+                s = cstreams[k]
+                if done is not None:
+                    s.wait_event(done)      # the previous step no longer reads it
+                with torch.cuda.stream(s):
+                    dev_bufs[k].copy_(v, non_blocking=True)
+                stream.wait_stream(s)
             step(sp)
+            done = torch.cuda.Event()
+            done.record(stream)
             for k in outs:
-                host[k].copy_(dev_bufs[k], non_blocking=True)
+                s = cstreams[k]
+                s.wait_event(done)
+                with torch.cuda.stream(s):
+                    host[k].copy_(dev_bufs[k], non_blocking=True)
+        for s in cstreams.values():
+            stream.wait_stream(s)
         e1.record(stream)
         barrier()
         t = torch.tensor([e0.elapsed_time(e1)], dtype=torch.float64, device=dev)
@@ -422,7 +442,8 @@ def run_pmx(args, rank, world, local_rank):
         e2e = {'value': world * N * ke / (float(t) / 1e3), 'unit': UNIT,
                'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
                'steps': ke, 'path': 'pmx_nbody_step + pmx_nbody_adj_step (C ABI), pinned host '
-                                    'buffers copied in and out every step'}
+                                    'buffers copied in and out every step (one copy stream '
+                                    'per buffer)'}
 
     if rank != 0:
         return

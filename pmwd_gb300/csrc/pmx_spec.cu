@@ -196,13 +196,20 @@ __device__ __forceinline__ float warp_sumf(float v) {
 // One warp per (x, y) row of n2h cells, lanes on consecutive kz (coalesced
 // loads); per 32 cells, shuffle sums per distinct bin (usually one or two)
 // and one float64 shared-memory add per bin.  CROSS: F conj(G); GEOM: also
-// the sums of k N and N; WIN: sinc^-deconv windows.
-template <bool CROSS, bool GEOM, bool WIN>
+// the sums of k N and N; WIN: sinc^-deconv windows.  PRIV (few bins): every
+// warp owns its own bin array, so the per-bin adds are plain stores of one
+// lane instead of float64 atomics that all warps of the block contend for;
+// the arrays are summed at the end.
+constexpr int PRIV_BINS = 64;
+
+template <bool CROSS, bool GEOM, bool WIN, bool PRIV>
 __global__ void __launch_bounds__(ST) k_powspec_rows(Pow2Args a) {
-    extern __shared__ double sb[];  // 4 doubles per bin
-    for (int i = threadIdx.x; i < 4 * a.nbin; i += ST) sb[i] = 0.0;
+    extern __shared__ double sbase[];  // 4 doubles per bin (per warp with PRIV)
+    const int nacc = (PRIV ? ST / 32 : 1) * 4 * a.nbin;
+    for (int i = threadIdx.x; i < nacc; i += ST) sbase[i] = 0.0;
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    double *sb = PRIV ? sbase + (threadIdx.x >> 5) * 4 * a.nbin : sbase;
     const int n2h = (int)a.n2h, az = (int)a.az;
     const int64_t nrows = a.n0 * a.n1;
     const int64_t wstride = (int64_t)gridDim.x * (ST / 32);
@@ -250,6 +257,21 @@ __global__ void __launch_bounds__(ST) k_powspec_rows(Pow2Args a) {
                     }
                 }
             }
+            // many distinct bins in these 32 cells (fine linear bins): each
+            // lane adds its own values; few: shuffle sums per bin
+            const unsigned peers = __match_any_sync(0xffffffffu, b);
+            const int ndist = __popc(__ballot_sync(0xffffffffu, lane == __ffs(peers) - 1));
+            if (ndist > 4) {
+                if (b < a.nbin) {
+                    atomicAdd(sb + 4 * b + 1, (double)pr);
+                    if (CROSS) atomicAdd(sb + 4 * b + 2, (double)pi);
+                    if (GEOM) {
+                        atomicAdd(sb + 4 * b, kn);
+                        atomicAdd(sb + 4 * b + 3, nn);
+                    }
+                }
+                continue;
+            }
             unsigned pending = __ballot_sync(0xffffffffu, b < a.nbin);
             while (pending) {
                 const int src = __ffs(pending) - 1;
@@ -263,35 +285,72 @@ __global__ void __launch_bounds__(ST) k_powspec_rows(Pow2Args a) {
                     sn = warp_sum(mine ? nn : 0.0);
                 }
                 if (lane == src) {
-                    atomicAdd(sb + 4 * bb + 1, (double)spr);
-                    if (CROSS) atomicAdd(sb + 4 * bb + 2, (double)spi);
-                    if (GEOM) {
-                        atomicAdd(sb + 4 * bb, sk);
-                        atomicAdd(sb + 4 * bb + 3, sn);
+                    if (PRIV) {  // this warp's array: one lane at a time
+                        sb[4 * bb + 1] += (double)spr;
+                        if (CROSS) sb[4 * bb + 2] += (double)spi;
+                        if (GEOM) {
+                            sb[4 * bb] += sk;
+                            sb[4 * bb + 3] += sn;
+                        }
+                    } else {
+                        atomicAdd(sb + 4 * bb + 1, (double)spr);
+                        if (CROSS) atomicAdd(sb + 4 * bb + 2, (double)spi);
+                        if (GEOM) {
+                            atomicAdd(sb + 4 * bb, sk);
+                            atomicAdd(sb + 4 * bb + 3, sn);
+                        }
                     }
                 }
                 pending &= ~__ballot_sync(0xffffffffu, mine);
             }
+            if (PRIV) __syncwarp();  // the next chunk's adds see these
         }
     }
     __syncthreads();
     for (int b = threadIdx.x; b < a.nbin; b += ST) {
+        double acc[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[c] = sbase[4 * b + c];
+        if (PRIV)
+            for (int w = 1; w < ST / 32; ++w)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[c] += sbase[w * 4 * a.nbin + 4 * b + c];
         if (GEOM) {
-            atomicAdd(a.ksum + b, sb[4 * b]);
-            atomicAdd(a.nsum + b, sb[4 * b + 3]);
+            atomicAdd(a.ksum + b, acc[0]);
+            atomicAdd(a.nsum + b, acc[3]);
         }
-        atomicAdd(a.psum + 2 * b, sb[4 * b + 1]);
-        if (CROSS) atomicAdd(a.psum + 2 * b + 1, sb[4 * b + 2]);
+        atomicAdd(a.psum + 2 * b, acc[1]);
+        if (CROSS) atomicAdd(a.psum + 2 * b + 1, acc[2]);
+    }
+}
+
+// Dynamic shared memory above the default 48 KB needs the opt-in attribute.
+template <class K>
+void allow_smem(K *kern, size_t sm) {
+    if (sm > 48 * 1024)
+        cudaFuncSetAttribute(reinterpret_cast<const void *>(kern),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+}
+
+template <bool CROSS, bool GEOM, bool PRIV>
+void launch_rows_p(const Pow2Args &p, cudaStream_t s) {
+    const size_t sm = (PRIV ? ST / 32 : 1) * 4 * (size_t)p.nbin * sizeof(double);
+    const int grid = stride_grid(p.n0 * p.n1 * 32, ST, 8);
+    if (p.wx) {
+        allow_smem(k_powspec_rows<CROSS, GEOM, true, PRIV>, sm);
+        k_powspec_rows<CROSS, GEOM, true, PRIV><<<grid, ST, sm, s>>>(p);
+    } else {
+        allow_smem(k_powspec_rows<CROSS, GEOM, false, PRIV>, sm);
+        k_powspec_rows<CROSS, GEOM, false, PRIV><<<grid, ST, sm, s>>>(p);
     }
 }
 
 template <bool CROSS, bool GEOM>
-void launch_rows(const Pow2Args &p, size_t sm, cudaStream_t s) {
-    const int grid = stride_grid(p.n0 * p.n1 * 32, ST, 8);
-    if (p.wx)
-        k_powspec_rows<CROSS, GEOM, true><<<grid, ST, sm, s>>>(p);
+void launch_rows(const Pow2Args &p, cudaStream_t s) {
+    if (p.nbin <= PRIV_BINS)
+        launch_rows_p<CROSS, GEOM, true>(p, s);
     else
-        k_powspec_rows<CROSS, GEOM, false><<<grid, ST, sm, s>>>(p);
+        launch_rows_p<CROSS, GEOM, false>(p, s);
 }
 
 bool is_pow2(int64_t n) { return n > 0 && (n & (n - 1)) == 0; }
@@ -387,13 +446,12 @@ extern "C" int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
             p.wy = w + a.n0;
             p.wz = w + a.n0 + a.n1;
         }
-        const size_t sm = 4 * nbin * sizeof(double);
         if (a.G) {
-            if (ksum) launch_rows<true, true>(p, sm, s);
-            else launch_rows<true, false>(p, sm, s);
+            if (ksum) launch_rows<true, true>(p, s);
+            else launch_rows<true, false>(p, s);
         } else {
-            if (ksum) launch_rows<false, true>(p, sm, s);
-            else launch_rows<false, false>(p, sm, s);
+            if (ksum) launch_rows<false, true>(p, s);
+            else launch_rows<false, false>(p, s);
         }
         PMX_LAUNCH_CHECK("k_powspec_rows");
         PMX_CUDA(cudaFreeAsync(scr, s));
@@ -402,6 +460,7 @@ extern "C" int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
     if (!ksum) return fail(PMX_ERR_ARG, "ksum/nsum may be NULL only for power-of-two grids <= 2048");
     const int grid = stride_grid(a.Mc, ST, 4);
     if (nbin <= SMEM_BINS) {
+        allow_smem(k_powspec<true>, 4 * nbin * sizeof(double));
         k_powspec<true><<<grid, ST, 4 * nbin * sizeof(double), s>>>(a);
     } else {
         k_powspec<false><<<grid, ST, 0, s>>>(a);

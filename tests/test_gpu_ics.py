@@ -56,10 +56,13 @@ def test_powspec_matches_oracle(cuda, ic_case):
 
 
 @pytest.mark.parametrize('shape, bins', [((32, 32, 32), 1), ((24, 20, 15), 1j / 4),
-                                         ((40, 36, 18), 2)])
+                                         ((40, 36, 18), 2), ((64, 64, 64), 0.5),
+                                         ((64, 64, 64), 0.03)])
 def test_powspec_kernel_matches_oracle(cuda, shape, bins):
     """pmx_powspec_bin (one pass over the complex64 spectrum) against the
-    oracle's digitize/bincount, linear and log bins, odd and even grids."""
+    oracle's digitize/bincount, linear and log bins, odd and even grids; the
+    power-of-two grids cover warp-private bins (29), block-shared bins (112)
+    and block-shared bins above 48 KB of shared memory (1848)."""
     from pmwd_gb300.spec_util import powspec
     f = np.random.default_rng(4).normal(size=shape).astype(np.float32)
     k_o, P_o, N_o, b_o = ics.powspec(f, 1.5, bins=bins)
