@@ -63,6 +63,9 @@ def parse():
                     help='scatter/gather contention stress: 256^3 particles, 256^3 mesh, 64 Mpc/h '
                          'box evolved to a=1 vs the same particles on the lattice')
     ap.add_argument('--serve-steps', default='10,100')
+    ap.add_argument('--published', action='store_true',
+                    help="pmwd's own timing table (perf.py): growth, 2LPT and N-body per step "
+                         "for ptcl grids 32^3..512^3 at mesh x1 and x2")
     return ap.parse_args()
 
 
@@ -620,6 +623,81 @@ def run_contention(args):
     print(json.dumps(line), flush=True)
 
 
+# pmwd's own timing table on an H100 PCIe (docs/papers/adjoint/perf.txt,
+# made by docs/papers/adjoint/perf.py): rows growth tables, 2LPT, N-body per
+# step at mesh factor 1 and 2; columns particle grids 32^3 .. 512^3; seconds.
+PUBLISHED_PERF = {
+    'growth': (9.656670968979597e-03, 9.563866071403027e-03, 9.559712023474276e-03,
+               9.568694978952408e-03, 9.575393050909042e-03),
+    'lpt': (7.556179771199822e-04, 7.496170001104474e-04, 1.957484055310488e-03,
+            1.269906898960472e-02, 9.726452908944339e-02),
+    'nbody_mesh1': (7.354481240327004e-04, 7.306391089514364e-04, 1.220740359713091e-03,
+                    7.984881642187247e-03, 9.461856014058867e-02),
+    'nbody_mesh2': (7.260151724040043e-04, 7.381303748843493e-04, 2.829991937687736e-03,
+                    2.185595865739742e-02, 2.074725039365148e-01),
+}
+
+
+def run_published(args):
+    """pmwd's own performance table (perf.py) through this package's API:
+    for particle grids 32^3 .. 512^3 (spacing 1 Mpc/h, 63 steps from
+    a = 1/64) and mesh factors 1 and 2, the minimum wall time of the growth
+    tables (boltzmann), of 2LPT from the linear modes, and of a whole
+    forward N-body run divided by its 64 force evaluations, each beside the
+    H100 figure.  Timing as perf.py: wall clock around a call that waits
+    for the device, minimum over repeats."""
+    import torch
+    import pmwd_gb300 as pg
+    torch.cuda.set_device(0)
+    dev = torch.device('cuda', 0)
+    sides = (32, 64, 128, 256, 512)
+    out = {}
+
+    def best(fn, reps):
+        ts = []
+        for _ in range(reps + 1):   # the first call warms up (plans, workspaces)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts[1:])
+
+    for mf in (1, 2):
+        for c, side in enumerate(sides):
+            conf = pg.Configuration(1.0, (side,) * 3, mesh_shape=mf)
+            reps = 3 if side >= 512 else 5
+            with torch.no_grad():
+                cosmo0 = pg.SimpleLCDM(conf)
+                t_growth = best(lambda: pg.boltzmann(cosmo0, conf, varlin=False), reps)
+                cosmo = pg.boltzmann(cosmo0, conf)
+                modes = pg.white_noise(0, conf, device=dev)
+                t_lpt = best(lambda: pg.lpt(pg.linear_modes(modes, cosmo, conf), cosmo, conf), reps)
+                ptcl, obs = pg.lpt(pg.linear_modes(modes, cosmo, conf), cosmo, conf)
+                nforce = 1 + conf.a_nbody_num
+                t_nb = best(lambda: pg.nbody(ptcl, obs, cosmo, conf), reps) / nforce
+            key = f'{side}^3 mesh x{mf}'
+            row = {'nbody_ms_per_step': 1e3 * t_nb,
+                   'nbody_published_ms': 1e3 * PUBLISHED_PERF[f'nbody_mesh{mf}'][c],
+                   'nbody_speedup': PUBLISHED_PERF[f'nbody_mesh{mf}'][c] / t_nb,
+                   'ptcl_steps_per_s': side ** 3 / t_nb}
+            if mf == 2:   # perf.py's growth and 2LPT rows come from its mesh x2 pass
+                row.update({'lpt_ms': 1e3 * t_lpt, 'lpt_published_ms': 1e3 * PUBLISHED_PERF['lpt'][c],
+                            'growth_ms': 1e3 * t_growth,
+                            'growth_published_ms': 1e3 * PUBLISHED_PERF['growth'][c]})
+            out[key] = row
+            print(json.dumps({key: row}), file=sys.stderr, flush=True)
+            del ptcl, obs, modes
+            torch.cuda.empty_cache()
+    line = {'metric': "pmwd's published timing table (perf.py) on GB300", 'unit': 'ms',
+            'config': {'workload': 'ptcl grids 32^3..512^3, spacing 1 Mpc/h, mesh x1 and x2, '
+                                   '63 steps from a=1/64, 2LPT, growth tables',
+                       'published_hardware': 'H100 PCIe (docs/papers/adjoint/perf.txt)',
+                       'timing': 'wall clock, min over repeats, device synchronised'},
+            'rows': out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get('RANK', 0))
@@ -635,6 +713,10 @@ def main():
     if args.contention:
         if rank == 0:
             run_contention(args)
+        return
+    if args.published:
+        if rank == 0:
+            run_published(args)
         return
     if world > 1:
         import torch

@@ -285,6 +285,21 @@ int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
                     double *ksum, double *psum, double *nsum, void *stream);
 
 /* --------------------------------------------------------------------------
+ * Growth functions (host)
+ * ------------------------------------------------------------------------ */
+
+/* Integrates the growth ODEs of boltzmann.py:196-203 (replaces the odeint
+ * call of growth_integ, boltzmann.py:163-229) on the host with an adaptive
+ * Dormand-Prince 5(4) method, for nparam parameter sets params[4 p + (0..3)]
+ * = (Omega_m, Omega_k, w_0, w_a), from lna[0] (initial state G1 = 1,
+ * G1' = 0, G2 = 3/7, G2' = 0) through the increasing points lna[0..num).
+ * Writes y[(s nparam + p) 4 + i] = (G1, dG1/dlna, G2, dG2/dlna) at lna[s]
+ * and dy, its derivative with respect to lna there.  Host memory only; no
+ * GPU is needed. */
+int pmx_growth_ode(const double *params, int64_t nparam, const double *lna,
+                   int64_t num, double rtol, double atol, double *y, double *dy);
+
+/* --------------------------------------------------------------------------
  * Stage profiler (no counterpart in pmwd, which only times whole jitted
  * calls with timeit): CUDA events around each stage of the force and step
  * entry points of one workspace.

@@ -5,7 +5,8 @@ functions, linear power and top-hat variance (pmwd/boltzmann.py:1-455).
 * ``growth_integ``  the 1st/2nd-order LPT growth ODEs of boltzmann.py:163-229.
   The reference integrates them with its own adaptive Dormand-Prince
   ``odeint`` (ode_util.py) and differentiates through an adjoint ODE; here
-  SciPy's DOP853 integrates all the systems needed at once -- the nominal
+  libpmx's host Dormand-Prince 5(4) integrator (``pmx_growth_ode``, the same
+  method in C++) integrates all the systems needed at once -- the nominal
   parameters plus +/- perturbations of (Omega_m, Omega_k, w_0, w_a) on a
   shared step sequence -- and the table's parameter Jacobian is the central
   difference of those solutions.  ``GrowthTable`` exposes that Jacobian to
@@ -13,12 +14,13 @@ functions, linear power and top-hat variance (pmwd/boltzmann.py:1-455).
 * ``growth``, ``linear_power``, ``varlin``, ``boltzmann`` as in the reference.
 """
 
+import ctypes
 import math
 
 import numpy as np
 import torch
-from scipy.integrate import solve_ivp
 
+from . import _lib
 from .cosmology import E2, H_deriv, Omega_m_a
 
 DT = torch.float64
@@ -129,27 +131,9 @@ def transfer(k, cosmo, conf):
 _GROWTH_PARAMS = ('Omega_m', 'Omega_k', 'w_0', 'w_a')
 
 
-def _rhs_np(lna, y, Om, Ok, w0, wa):
-    """Growth ODEs of boltzmann.py:196-203 for a batch of parameter sets."""
-    a = math.exp(lna)
-    Ode = 1 - (Om + Ok)
-    p = -3 * (1 + w0 + wa)
-    q = -3 * wa
-    de = a ** p * np.exp(q * (1 - a))
-    E2 = Om * a ** -3 + Ok * a ** -2 + Ode * de
-    dlnH = 0.5 * (-3 * Om * a ** -3 - 2 * Ok * a ** -2 + Ode * de * (p - q * a)) / E2
-    Of = 1.5 * Om / (a ** 3 * E2)
-    y = y.reshape(-1, 4)
-    G1, G1p, G2, G2p = y[:, 0], y[:, 1], y[:, 2], y[:, 3]
-    G1pp = -(3 + dlnH - Of) * G1 - (4 + dlnH) * G1p
-    G2pp = Of * G1 ** 2 - (8 + 2 * dlnH - Of) * G2 - (6 + dlnH) * G2p
-    return np.stack([G1p, G1pp, G2p, G2pp], axis=1).reshape(-1)
-
-
 def _growth_tables_np(params, conf, rtol=1e-11, atol=1e-13):
     """Tables (P, 2, 3, num_a) for P parameter rows (Om, Ok, w0, wa)."""
     params = np.asarray(params, dtype=np.float64)
-    Om, Ok, w0, wa = params.T
     eps = np.finfo(np.float64).eps
     a_ic = 0.5 * np.cbrt(eps)
     if a_ic >= conf.a_lpt_step:
@@ -158,14 +142,14 @@ def _growth_tables_np(params, conf, rtol=1e-11, atol=1e-13):
     a[0] = a_ic
     lna = np.log(a)
     P = params.shape[0]
-    y0 = np.tile(np.array([1.0, 0.0, 3 / 7, 0.0]), P)
-    sol = solve_ivp(_rhs_np, (lna[0], lna[-1]), y0, method='DOP853', t_eval=lna,
-                    rtol=rtol, atol=atol, args=(Om, Ok, w0, wa))
-    if not sol.success:
-        raise RuntimeError(f'growth ODE failed: {sol.message}')
-    Y = sol.y.T.reshape(len(lna), P, 4)                                  # (num_a, P, 4)
-    Yd = np.stack([_rhs_np(t, y.reshape(-1), Om, Ok, w0, wa).reshape(P, 4)
-                   for t, y in zip(lna, Y)])                              # (num_a, P, 4)
+    # Dormand-Prince 5(4) in libpmx (host code): y and dy/dlna at every lna
+    Y = np.empty((len(lna), P, 4))                                       # (num_a, P, 4)
+    Yd = np.empty((len(lna), P, 4))
+    prm = np.ascontiguousarray(params)
+    lna = np.ascontiguousarray(lna)
+    f = lambda x: x.ctypes.data_as(ctypes.c_void_p)
+    _lib.check(_lib.load().pmx_growth_ode(f(prm), P, f(lna), len(lna), rtol, atol, f(Y), f(Yd)),
+               'pmx_growth_ode')
     G = np.stack([Y[..., 0:2], Y[..., 2:4]], axis=2)                      # (num_a, P, 2, 2)
     Gpp = np.stack([Yd[..., 1], Yd[..., 3]], axis=2)[..., None]          # (num_a, P, 2, 1)
     G = np.concatenate((G, Gpp), axis=3)                                  # (num_a, P, 2, 3)

@@ -26,9 +26,36 @@ def _strain(kvec, i, j, pot, conf):
     return fftinv(strain, shape=conf.ptcl_grid_shape).to(torch.float32)
 
 
+def _nyq_zeroed(k, conf):
+    nyquist = math.pi / conf.ptcl_spacing
+    eps = nyquist * torch.finfo(torch.float32).eps
+    return torch.where(torch.abs(torch.abs(k) - nyquist) <= eps, torch.zeros_like(k), k)
+
+
+def _L3(kvec, pot, conf):
+    """2nd-order source of one potential in 3-D (lpt.py:40-76 with m = n):
+    the six strain fields come from one batched inverse FFT (each diagonal
+    strain once), and the products are summed in the reference's order,
+    L = phi_00 phi_22 + phi_00 phi_11 + phi_11 phi_22
+        - phi_01^2 - phi_02^2 - phi_12^2."""
+    kz = [_nyq_zeroed(k, conf) for k in kvec]
+    pairs = ((0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2))
+    spec = torch.stack([-(kvec[i] if i == j else kz[i]) * (kvec[j] if i == j else kz[j]) * pot
+                        for i, j in pairs])
+    phi = fftinv(spec, shape=conf.ptcl_grid_shape, axes=(-3, -2, -1)).to(torch.float32)
+    L = phi[0] * phi[2]
+    L = torch.addcmul(L, phi[0], phi[1])
+    L = torch.addcmul(L, phi[1], phi[2])
+    for c in (3, 4, 5):
+        L = torch.addcmul(L, phi[c], phi[c], value=-1)
+    return L
+
+
 def _L(kvec, pot_m, pot_n, conf):
     """2nd-order source (lpt.py:40-76)."""
     m_eq_n = pot_n is None
+    if m_eq_n and conf.dim == 3:
+        return _L3(kvec, pot_m, conf)
     if m_eq_n:
         pot_n = pot_m
     L = torch.zeros(conf.ptcl_grid_shape, dtype=torch.float32, device=pot_m.device)
@@ -91,19 +118,24 @@ def lpt(modes, cosmo, conf):
 
     a = conf.a_start
     ptcl = Particles.gen_grid(conf, vel=True, device=dev)
-    disp, vel = ptcl.disp, ptcl.vel
+    if conf.lpt_order == 0:
+        return ptcl, None
+    # every displacement field of every order from one batched inverse FFT
+    grads = torch.stack([neg_grad(k, pot[o], conf.ptcl_spacing)
+                         for o in range(conf.lpt_order) for k in kvec])
+    grads = fftinv(grads, shape=conf.ptcl_grid_shape,
+                   axes=tuple(range(-conf.dim, 0))).to(torch.float32)
+    grads = grads.reshape(conf.lpt_order, conf.dim, -1)
+    # columns (dim, n): disp_i += D_m g_mi, vel_i += a^2 H dD_m/dlna g_mi,
+    # order by order as the reference accumulates them
+    disp, vel = ptcl.disp.t(), ptcl.vel.t()
     for order in range(1, 1 + conf.lpt_order):
         D = growth(a, cosmo, conf, order=order)
         dD_dlna = growth(a, cosmo, conf, order=order, deriv=1)
         a2HDp = a ** 2 * torch.sqrt(E2(a, cosmo)) * dD_dlna
         D = D.to(torch.float32).to(dev)
         a2HDp = a2HDp.to(torch.float32).to(dev)
-        cols_d, cols_v = [], []
-        for i, k in enumerate(kvec):
-            g = neg_grad(k, pot[order - 1], conf.ptcl_spacing)
-            g = fftinv(g, shape=conf.ptcl_grid_shape).to(torch.float32).reshape(-1)
-            cols_d.append(disp[:, i] + D * g)
-            cols_v.append(vel[:, i] + a2HDp * g)
-        disp = torch.stack(cols_d, dim=1)
-        vel = torch.stack(cols_v, dim=1)
-    return ptcl.replace(disp=disp, vel=vel), None
+        g = grads[order - 1]
+        disp = disp + D * g
+        vel = vel + a2HDp * g
+    return ptcl.replace(disp=disp.t().contiguous(), vel=vel.t().contiguous()), None

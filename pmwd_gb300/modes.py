@@ -6,6 +6,8 @@ machine; the reference draws JAX threefry normals instead, so realisations
 differ from the reference's while the distribution is the same.
 """
 
+import math
+
 import numpy as np
 import torch
 
@@ -42,16 +44,49 @@ class _SafeSqrt(torch.autograd.Function):
                            torch.zeros_like(g))
 
 
+def _mode_index(shape, device):
+    """For power-of-two grids: the integer m with k^2 = (2 pi / spacing)^2 m / D,
+    D = max(n)^2, of every rfft mode, and D.  fftfreq values are i / n_a, so
+    k^2 (2 pi / spacing)^-2 = sum_a i_a^2 / n_a^2 = m / D exactly.  None for
+    other grids."""
+    if not all(n > 1 and n & (n - 1) == 0 for n in shape):
+        return None
+    D = max(shape) ** 2
+    idx = []
+    for ax, n in enumerate(shape):
+        i = torch.arange(n // 2 + 1 if ax == len(shape) - 1 else n, device=device)
+        if ax < len(shape) - 1:
+            i = torch.where(i < (n + 1) // 2, i, i - n)
+        m = (i * i * (D // (n * n))).to(torch.int32)
+        idx.append(m.reshape((1,) * ax + (-1,) + (1,) * (len(shape) - ax - 1)))
+    # the largest index, |i_a| = n_a / 2 on every axis, is dim D / 4
+    return sum(idx), D, len(shape) * D // 4
+
+
 def linear_modes(modes, cosmo, conf, a=None, real=False):
     """Linear matter overdensity modes (modes.py:67-117): Fourier modes times
-    sqrt(V P_lin(k)); optionally back to real space (dimensionless)."""
+    sqrt(V P_lin(k)); optionally back to real space (dimensionless).
+
+    P_lin depends on |k| only: on power-of-two grids sqrt(V P_lin) is
+    evaluated once per distinct k^2 (float64 math, float32 result, as per
+    mode) and gathered, instead of evaluating the float64 transfer function
+    and power law at every mode."""
     dev = modes.device
-    kvec = fftfreq(conf.ptcl_grid_shape, conf.ptcl_spacing, dtype=torch.float32, device=dev)
-    k = torch.sqrt(sum(kk ** 2 for kk in kvec))
-    Plin = linear_power(k, a, cosmo, conf).to(torch.float32)
+    mi = _mode_index(conf.ptcl_grid_shape, dev)
+    if mi is not None:
+        m, D, mmax = mi
+        mv = torch.arange(mmax + 1, device=dev, dtype=torch.float64)
+        k = (2 * math.pi / conf.ptcl_spacing) * torch.sqrt(mv / D)
+        Plin = linear_power(k, a, cosmo, conf).to(torch.float32)
+        amp = _SafeSqrt.apply(Plin * conf.box_vol)[m.long()]
+    else:
+        kvec = fftfreq(conf.ptcl_grid_shape, conf.ptcl_spacing, dtype=torch.float32, device=dev)
+        k = torch.sqrt(sum(kk ** 2 for kk in kvec))
+        Plin = linear_power(k, a, cosmo, conf).to(torch.float32)
+        amp = _SafeSqrt.apply(Plin * conf.box_vol)
     if not torch.is_complex(modes):
         modes = fftfwd(modes, norm='ortho')
-    modes = modes * _SafeSqrt.apply(Plin * conf.box_vol)
+    modes = modes * amp
     if real:
         modes = fftinv(modes, shape=conf.ptcl_grid_shape, norm=conf.ptcl_spacing)
     return modes

@@ -12,6 +12,16 @@ def pytest_configure(config):
     config.addinivalue_line('markers', 'gpu: needs a CUDA GPU (GB300) and the built libpmx.so')
 
 
+@pytest.fixture(scope='session', autouse=True)
+def libpmx():
+    """libpmx.so, built in-tree when missing (nvcc cross-compiles without a
+    GPU): the host-side growth integrator lives in it too."""
+    from pmwd_gb300 import _build, _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        _build.build()
+    return _lib.load()
+
+
 @pytest.fixture(scope='session')
 def cuda():
     import torch

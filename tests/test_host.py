@@ -55,6 +55,33 @@ def test_background_and_tables(both):
                                rtol=2e-4)
 
 
+@pytest.mark.parametrize('pars', [dict(Omega_m=0.25, Omega_k=0.05, w_0=-0.9, w_a=0.1),
+                                  dict(Omega_m=0.35, Omega_k=-0.03, w_0=-1.1, w_a=-0.2)])
+def test_growth_tables_other_backgrounds(pars):
+    """The host Dormand-Prince integrator (pmx_growth_ode) against the
+    oracle's Radau solution with curvature and evolving dark energy."""
+    oconf = oc.OConf(2.0, (16, 16, 16), 2, a_nbody_maxstep=1 / 16)
+    gconf = pg.Configuration(2.0, (16, 16, 16), 2, a_nbody_maxstep=1 / 16)
+    ocos = oc.simple_lcdm(**pars)
+    gcos = pg.SimpleLCDM(gconf).replace(**{(k if k == 'Omega_m' else k + '_'):
+                                           torch.tensor(v, dtype=torch.float64)
+                                           for k, v in pars.items()})
+    gcos = pg.boltzmann(gcos, gconf, transfer=False, varlin=False)
+    np.testing.assert_allclose(gcos.growth.numpy(), oc.growth_table(ocos, oconf), rtol=2e-8,
+                               atol=1e-12)
+
+
+def test_growth_ode_rejects_bad_arguments():
+    from pmwd_gb300 import _lib
+    lib = _lib.load()
+    prm = np.array([0.3, 0.0, -1.0, 0.0])
+    y = np.empty(8)
+    f = lambda x: x.ctypes.data_as(__import__('ctypes').c_void_p)
+    down = np.array([0.0, -1.0])
+    assert lib.pmx_growth_ode(f(prm), 1, f(down), 2, 1e-10, 1e-12, f(y), f(y)) != 0
+    assert lib.pmx_growth_ode(f(prm), 1, f(np.array([-1.0, 0.0])), 2, 0.0, 1e-12, f(y), f(y)) != 0
+
+
 def test_growth_jacobian_matches_finite_differences(both):
     _, gconf, _, _ = both
     Om = torch.tensor(0.3, dtype=torch.float64, requires_grad=True)
