@@ -2,6 +2,8 @@
 torch on the GPU (cuFFT through torch.fft; autograd gives its VJP)."""
 
 import math
+import threading
+from collections import OrderedDict
 from itertools import combinations, permutations
 
 import torch
@@ -95,47 +97,160 @@ def _M(kvec, pot, conf):
     return M
 
 
-def lpt(modes, cosmo, conf):
-    """LPT displacements and velocities at conf.a_start (lpt.py:136-212).
+def _growth_factors(cosmo, conf):
+    """(lpt_order, 2) float32 host tensor of (D_m, a^2 H dD_m/dlna) at
+    conf.a_start, the factors of lpt.py:197-210 (differentiable in the
+    cosmology)."""
+    a = conf.a_start
+    rows = []
+    for order in range(1, 1 + conf.lpt_order):
+        D = growth(a, cosmo, conf, order=order)
+        dD_dlna = growth(a, cosmo, conf, order=order, deriv=1)
+        a2HDp = a ** 2 * torch.sqrt(E2(a, cosmo)) * dD_dlna
+        rows.append(torch.stack([D.reshape(()), a2HDp.reshape(())]))
+    return torch.stack(rows).to(torch.float32)
 
-    Returns ``(ptcl, None)`` with particles on the Lagrangian grid.
-    """
-    if conf.dim not in (1, 2, 3):
-        raise ValueError(f'dim={conf.dim} not supported')
-    if conf.lpt_order not in (0, 1, 2, 3):
-        raise ValueError(f'lpt_order={conf.lpt_order} not supported')
-    dev = modes.device
+
+def _lpt_device(modes, fac, kvec, disp0, vel0, conf):
+    """The device work of lpt (lpt.py:136-212) for lpt_order >= 1: the
+    potentials, the 2nd-order source, and every displacement field of every
+    order from one batched inverse FFT; fac (lpt_order, 2) float32 on the
+    device.  Returns disp, vel as (dim, n) columns: disp_i += D_m g_mi,
+    vel_i += a^2 H dD_m/dlna g_mi, order by order as the reference
+    accumulates them."""
     modes = modes / conf.ptcl_cell_vol
-    kvec = fftfreq(conf.ptcl_grid_shape, conf.ptcl_spacing, dtype=torch.float32, device=dev)
-    pot = []
-    if conf.lpt_order > 0:
-        pot.append(laplace(kvec, modes, cosmo))
+    pot = [laplace(kvec, modes)]
     if conf.lpt_order > 1:
         src_2 = fftfwd(_L(kvec, pot[0], None, conf))
-        pot.append(laplace(kvec, src_2, cosmo))
-    if conf.lpt_order > 2:
-        raise NotImplementedError('TODO')
-
-    a = conf.a_start
-    ptcl = Particles.gen_grid(conf, vel=True, device=dev)
-    if conf.lpt_order == 0:
-        return ptcl, None
-    # every displacement field of every order from one batched inverse FFT
+        pot.append(laplace(kvec, src_2))
     grads = torch.stack([neg_grad(k, pot[o], conf.ptcl_spacing)
                          for o in range(conf.lpt_order) for k in kvec])
     grads = fftinv(grads, shape=conf.ptcl_grid_shape,
                    axes=tuple(range(-conf.dim, 0))).to(torch.float32)
     grads = grads.reshape(conf.lpt_order, conf.dim, -1)
-    # columns (dim, n): disp_i += D_m g_mi, vel_i += a^2 H dD_m/dlna g_mi,
-    # order by order as the reference accumulates them
-    disp, vel = ptcl.disp.t(), ptcl.vel.t()
-    for order in range(1, 1 + conf.lpt_order):
-        D = growth(a, cosmo, conf, order=order)
-        dD_dlna = growth(a, cosmo, conf, order=order, deriv=1)
-        a2HDp = a ** 2 * torch.sqrt(E2(a, cosmo)) * dD_dlna
-        D = D.to(torch.float32).to(dev)
-        a2HDp = a2HDp.to(torch.float32).to(dev)
-        g = grads[order - 1]
-        disp = disp + D * g
-        vel = vel + a2HDp * g
+    disp, vel = disp0, vel0
+    for o in range(conf.lpt_order):
+        disp = disp + fac[o, 0] * grads[o]
+        vel = vel + fac[o, 1] * grads[o]
+    return disp, vel
+
+
+# CUDA-graph replay of _lpt_device for calls without gradients on small
+# grids, where launching ~10^3 small kernels one by one would cost more than
+# the transforms themselves.  One graph per (configuration, device); the
+# growth factors are a graph input, so a graph serves every cosmology.
+# Replays run on the graph's own stream under a lock, so concurrent callers
+# (the serving threads) never share the static buffers in flight.
+GRAPH_MAX_PTCL = 256 ** 3
+_GRAPHS = OrderedDict()
+_GRAPHS_MAX = 8
+_GRAPH_LOCK = threading.Lock()
+
+
+class _LptGraph:
+    def __init__(self, conf, dev, spec_shape):
+        self.conf, self.dev = conf, dev
+        self.stream = torch.cuda.Stream(dev)
+        self.modes = torch.zeros(spec_shape, dtype=torch.complex64, device=dev)
+        self.fac = torch.zeros((conf.lpt_order, 2), dtype=torch.float32, device=dev)
+        # pinned staging for the factors: a ring, each slot reused only after
+        # its last upload has completed
+        self.ring = [torch.zeros((conf.lpt_order, 2), dtype=torch.float32).pin_memory()
+                     for _ in range(4)]
+        self.ring_ev = [None] * 4
+        self.slot = 0
+        grid = Particles.gen_grid(conf, vel=True, device=dev)
+        self.pmid = grid.pmid
+        self.disp0, self.vel0 = grid.disp.t(), grid.vel.t()
+        self.kvec = fftfreq(conf.ptcl_grid_shape, conf.ptcl_spacing, dtype=torch.float32,
+                            device=dev)
+        cur = torch.cuda.current_stream(dev)
+        self.stream.wait_stream(cur)
+        with torch.no_grad():
+            with torch.cuda.stream(self.stream):
+                for _ in range(2):   # plans and allocator pools before capture
+                    _lpt_device(self.modes, self.fac, self.kvec, self.disp0, self.vel0, conf)
+            self.stream.synchronize()
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=self.stream,
+                                  capture_error_mode='thread_local'):
+                self.disp, self.vel = _lpt_device(self.modes, self.fac, self.kvec, self.disp0,
+                                                  self.vel0, conf)
+
+    def run(self, modes, fac):
+        cur = torch.cuda.current_stream(self.dev)
+        with _GRAPH_LOCK, torch.no_grad():
+            i = self.slot
+            self.slot = (i + 1) % len(self.ring)
+            if self.ring_ev[i] is not None:
+                self.ring_ev[i].synchronize()
+            self.ring[i].copy_(fac)
+            self.stream.wait_stream(cur)   # modes are ready
+            with torch.cuda.stream(self.stream):
+                self.fac.copy_(self.ring[i], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(self.stream)
+                self.ring_ev[i] = ev
+                self.modes.copy_(modes)
+                self.graph.replay()
+                out = (self.pmid.clone(), self.disp.t().contiguous(), self.vel.t().contiguous())
+        cur.wait_stream(self.stream)
+        for t in out:   # allocated on the graph's stream, used on the caller's
+            t.record_stream(cur)
+        modes.record_stream(self.stream)
+        return out
+
+
+def _graph_for(conf, modes):
+    key = (conf, modes.device.index)
+    with _GRAPH_LOCK:
+        g = _GRAPHS.get(key)
+        if g is not None:
+            _GRAPHS.move_to_end(key)
+            return g
+    g = _LptGraph(conf, modes.device, tuple(modes.shape))
+    with _GRAPH_LOCK:
+        _GRAPHS[key] = g
+        while len(_GRAPHS) > _GRAPHS_MAX:
+            _GRAPHS.popitem(last=False)
+    return g
+
+
+def _wants_graph(modes, cosmo, conf):
+    if not modes.is_cuda or conf.lpt_order < 1 or conf.ptcl_num > GRAPH_MAX_PTCL:
+        return False
+    if modes.dtype != torch.complex64 or tuple(modes.shape) != tuple(
+            conf.ptcl_grid_shape[:-1]) + (conf.ptcl_grid_shape[-1] // 2 + 1,):
+        return False
+    if not torch.is_grad_enabled():
+        return True
+    return not (modes.requires_grad or any(
+        torch.is_tensor(v) and v.requires_grad for v in vars(cosmo).values()))
+
+
+def lpt(modes, cosmo, conf):
+    """LPT displacements and velocities at conf.a_start (lpt.py:136-212).
+
+    Returns ``(ptcl, None)`` with particles on the Lagrangian grid.  Calls
+    that need no gradient, on grids up to 256^3, replay a CUDA graph of the
+    device work.
+    """
+    if conf.dim not in (1, 2, 3):
+        raise ValueError(f'dim={conf.dim} not supported')
+    if conf.lpt_order not in (0, 1, 2, 3):
+        raise ValueError(f'lpt_order={conf.lpt_order} not supported')
+    if conf.lpt_order > 2:
+        raise NotImplementedError('TODO')
+    dev = modes.device
+    if conf.lpt_order == 0:
+        return Particles.gen_grid(conf, vel=True, device=dev), None
+    if _wants_graph(modes, cosmo, conf):
+        with torch.no_grad():
+            fac = _growth_factors(cosmo, conf)
+        pmid, disp, vel = _graph_for(conf, modes).run(modes, fac)
+        return Particles(conf, pmid, disp, vel=vel), None
+    fac = _growth_factors(cosmo, conf).to(dev)
+    kvec = fftfreq(conf.ptcl_grid_shape, conf.ptcl_spacing, dtype=torch.float32, device=dev)
+    ptcl = Particles.gen_grid(conf, vel=True, device=dev)
+    disp, vel = _lpt_device(modes, fac, kvec, ptcl.disp.t(), ptcl.vel.t(), conf)
     return ptcl.replace(disp=disp.t().contiguous(), vel=vel.t().contiguous()), None

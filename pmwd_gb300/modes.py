@@ -44,7 +44,17 @@ class _SafeSqrt(torch.autograd.Function):
                            torch.zeros_like(g))
 
 
+_MODE_INDEX = {}
+
+
 def _mode_index(shape, device):
+    key = (tuple(shape), str(device))
+    if key not in _MODE_INDEX:
+        _MODE_INDEX[key] = _mode_index_build(shape, device)
+    return _MODE_INDEX[key]
+
+
+def _mode_index_build(shape, device):
     """For power-of-two grids: the integer m with k^2 = (2 pi / spacing)^2 m / D,
     D = max(n)^2, of every rfft mode, and D.  fftfreq values are i / n_a, so
     k^2 (2 pi / spacing)^-2 = sum_a i_a^2 / n_a^2 = m / D exactly.  None for
@@ -57,7 +67,7 @@ def _mode_index(shape, device):
         i = torch.arange(n // 2 + 1 if ax == len(shape) - 1 else n, device=device)
         if ax < len(shape) - 1:
             i = torch.where(i < (n + 1) // 2, i, i - n)
-        m = (i * i * (D // (n * n))).to(torch.int32)
+        m = (i * i * (D // (n * n))).to(torch.int32)   # dim D / 4 < 2^31 up to 2^15 per side
         idx.append(m.reshape((1,) * ax + (-1,) + (1,) * (len(shape) - ax - 1)))
     # the largest index, |i_a| = n_a / 2 on every axis, is dim D / 4
     return sum(idx), D, len(shape) * D // 4
@@ -74,11 +84,13 @@ def linear_modes(modes, cosmo, conf, a=None, real=False):
     dev = modes.device
     mi = _mode_index(conf.ptcl_grid_shape, dev)
     if mi is not None:
+        # the table is small (dim D / 4 + 1 entries): evaluated on the host,
+        # where the cosmology's tables and parameters live, then gathered
         m, D, mmax = mi
-        mv = torch.arange(mmax + 1, device=dev, dtype=torch.float64)
+        mv = torch.arange(mmax + 1, dtype=torch.float64)
         k = (2 * math.pi / conf.ptcl_spacing) * torch.sqrt(mv / D)
         Plin = linear_power(k, a, cosmo, conf).to(torch.float32)
-        amp = _SafeSqrt.apply(Plin * conf.box_vol)[m.long()]
+        amp = _SafeSqrt.apply(Plin * conf.box_vol).to(dev)[m]
     else:
         kvec = fftfreq(conf.ptcl_grid_shape, conf.ptcl_spacing, dtype=torch.float32, device=dev)
         k = torch.sqrt(sum(kk ** 2 for kk in kvec))

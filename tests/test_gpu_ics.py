@@ -96,6 +96,28 @@ def test_powspec_kernel_cross_deconv_batch(cuda, shape):
                 np.testing.assert_allclose(a.cpu().numpy(), b.numpy(), rtol=1e-6, atol=0)
 
 
+def test_lpt_graph_replay_matches_eager(cuda):
+    """Calls without gradients replay a CUDA graph of the 2LPT device work;
+    the graph takes the growth factors as an input, so one graph serves
+    several cosmologies.  It matches the eager path, which runs when the
+    modes need a gradient."""
+    import importlib
+    glpt = importlib.import_module('pmwd_gb300.lpt')
+    conf = pg.Configuration(2.0, (32, 32, 32), 2)
+    glpt._GRAPHS.clear()
+    for Om in (0.3, 0.25):
+        cos = pg.boltzmann(pg.SimpleLCDM(conf).replace(
+            Omega_m=torch.tensor(Om, dtype=torch.float64)), conf)
+        modes = pg.linear_modes(pg.white_noise(1, conf, device=cuda), cos, conf)
+        with torch.no_grad():
+            g, _ = pg.lpt(modes, cos, conf)
+        e, _ = pg.lpt(modes.clone().requires_grad_(True), cos, conf)
+        assert len(glpt._GRAPHS) == 1
+        assert torch.equal(g.pmid, e.pmid)
+        assert rel_l2(g.disp.cpu().numpy(), e.disp.detach().cpu().numpy()) < 1e-6
+        assert rel_l2(g.vel.cpu().numpy(), e.vel.detach().cpu().numpy()) < 1e-6
+
+
 def test_lpt_statistics_match_published(cuda):
     """docs/examples/quickstart.ipynb prints, for 256^3 particles, spacing 1,
     2x mesh, SimpleLCDM, after 2LPT at a=1/64: disp.std() = 0.105 and
