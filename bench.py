@@ -63,6 +63,9 @@ def parse():
                     help='scatter/gather contention stress: 256^3 particles, 256^3 mesh, 64 Mpc/h '
                          'box evolved to a=1 vs the same particles on the lattice')
     ap.add_argument('--serve-steps', default='10,100')
+    ap.add_argument('--gradient', action='store_true',
+                    help="the reference quickstart's gradient: 256^3 / 512^3 mesh, 63 steps, "
+                         "d var(dens - target) / d(modes, cosmology)")
     ap.add_argument('--published', action='store_true',
                     help="pmwd's own timing table (perf.py): growth, 2LPT and N-body per step "
                          "for ptcl grids 32^3..512^3 at mesh x1 and x2")
@@ -698,6 +701,70 @@ def run_published(args):
     print(json.dumps(line), flush=True)
 
 
+def run_gradient(args):
+    """The reference quickstart's gradient workload (docs/examples/
+    quickstart.ipynb): 256^3 particles, 512^3 mesh, spacing 1 Mpc/h, 63
+    steps; objective var(scatter(nbody(lpt(linear_modes(modes))))) - target)
+    with the target from another white-noise seed, differentiated with
+    respect to the real white-noise modes and the five SimpleLCDM parameters
+    (boltzmann included in the differentiated function).  Wall time of a
+    warm call, device synchronised; pmwd publishes 5.27 s on an H100 PCIe
+    (and 1.43 s for the forward model)."""
+    import torch
+    import pmwd_gb300 as pg
+    torch.cuda.set_device(0)
+    dev = torch.device('cuda', 0)
+    conf = pg.Configuration(1.0, (256,) * 3, mesh_shape=2)
+    names = ('A_s_1e9', 'n_s', 'Omega_m', 'Omega_b', 'h')
+    base = pg.SimpleLCDM(conf)
+
+    def model(modes, cosmo):
+        cosmo = pg.boltzmann(cosmo, conf)
+        modes = pg.linear_modes(modes, cosmo, conf)
+        ptcl, obs = pg.lpt(modes, cosmo, conf)
+        return pg.nbody(ptcl, obs, cosmo, conf)
+
+    with torch.no_grad():
+        ptcl, _ = model(pg.white_noise(0, conf, device=dev), base)
+        tgt = pg.scatter(ptcl, conf)
+    modes = pg.white_noise(1, conf, real=True, device=dev)
+
+    def obj_grad():
+        m = modes.clone().requires_grad_(True)
+        prm = {k: torch.tensor(float(getattr(base, k)), dtype=torch.float64, requires_grad=True)
+               for k in names}
+        ptcl, _ = model(m, base.replace(**prm))
+        loss = (pg.scatter(ptcl, conf) - tgt).var(correction=0)
+        loss.backward()
+        return float(loss), m.grad, {k: float(v.grad) for k, v in prm.items()}
+
+    def timed(fn, reps=3):
+        ts, out = [], None
+        for _ in range(reps + 1):   # the first call warms plans and workspaces
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts[1:]), out
+
+    with torch.no_grad():
+        t_fwd, _ = timed(lambda: model(modes, base))
+    t_grad, (loss, mgrad, cgrad) = timed(obj_grad)
+    line = {'metric': "quickstart gradient (pmwd's docs/examples/quickstart.ipynb)", 'unit': 's',
+            'config': {'workload': '256^3 ptcl, 512^3 mesh, spacing 1 Mpc/h, 63 steps; objective '
+                                   'var(scatter(nbody(lpt(linear_modes(modes)))) - target); '
+                                   'gradient w.r.t. white-noise modes and 5 cosmological parameters',
+                       'published_hardware': 'H100 PCIe (quickstart.ipynb)',
+                       'timing': 'wall clock of a warm call, min over 3, device synchronised'},
+            'gradient_s': t_grad, 'gradient_published_s': 5.27,
+            'gradient_speedup': 5.27 / t_grad,
+            'forward_model_s': t_fwd, 'forward_model_published_s': 1.43,
+            'loss': loss, 'modes_grad_std': float(mgrad.std()),
+            'cosmo_grad': cgrad}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get('RANK', 0))
@@ -717,6 +784,10 @@ def main():
     if args.published:
         if rank == 0:
             run_published(args)
+        return
+    if args.gradient:
+        if rank == 0:
+            run_gradient(args)
         return
     if world > 1:
         import torch
