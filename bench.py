@@ -736,7 +736,7 @@ def run_gradient(args):
         ptcl, _ = model(m, base.replace(**prm))
         loss = (pg.scatter(ptcl, conf) - tgt).var(correction=0)
         loss.backward()
-        return float(loss), m.grad, {k: float(v.grad) for k, v in prm.items()}
+        return float(loss.detach()), m.grad, {k: float(v.grad) for k, v in prm.items()}
 
     def timed(fn, reps=3):
         ts, out = [], None

@@ -1244,11 +1244,19 @@ int make_plan2d(cufftHandle *plan, int64_t n1, int64_t n2, cufftType type, int64
 // x-planes per 2-D cuFFT execution: PMX_SLAB if set, else 8, so that the
 // intermediate of every concurrent execution stays in L2 (the slab loops run
 // as captured CUDA graphs, which removes the per-call launch cost).
-int64_t choose_slab(int64_t n0) {
+// x-planes per slab execution of the (y, z) plane transforms: the smallest
+// power of two >= 8 whose complex planes reach 32 MB (8 planes at 1024^2,
+// every plane of meshes up to 128^3), so small meshes take a few large
+// cuFFT launches instead of many tiny ones.  PMX_SLAB overrides.
+int64_t choose_slab(int64_t n0, int64_t n1, int64_t n2) {
     const char *env = std::getenv("PMX_SLAB");
     int64_t S = 0;
     if (env) S = std::atoll(env);
-    if (S <= 0) S = 8;
+    if (S <= 0) {
+        const int64_t plane = n1 * (n2 / 2 + 1) * 8;
+        S = 8;
+        while (S < n0 && S * plane < ((int64_t)32 << 20)) S *= 2;
+    }
     if (S > n0) S = n0;
     while (S > 1 && n0 % S) S /= 2;
     if (S < 1) S = 1;
@@ -1400,7 +1408,7 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
         }
     }
     if (ws->xfast) {
-        ws->slab = choose_slab(ws->n0);
+        ws->slab = choose_slab(ws->n0, ws->n1, ws->n2);
         const int64_t S = ws->slab;
         if (!ws->plane) {
             const char *kenv = std::getenv("PMX_SLAB_CHAINS");

@@ -169,7 +169,7 @@ class _Job:
             self.adj = _nb.op_factors(_nb.adjoint_ops(conf), cosmo, conf)
             self.f_adj = self.adj.detach().to(torch.float32).numpy().reshape(-1, 3)
         self.spec = _lib.make_spec(3, conf.mesh_shape, conf.mesh_shape, conf.cell_size)
-        self.Om = float(cosmo.Omega_m)
+        self.Om = float(torch.as_tensor(cosmo.Omega_m).detach())
         lib = _lib.load()
         P = _lib.ptr
         _lib.check(lib.pmx_force(self.ws.handle, self.spec, P(self.pmid), P(self.disp),

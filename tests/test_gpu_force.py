@@ -293,10 +293,28 @@ def test_factors_match_oracle(nb_case):
     np.testing.assert_array_equal(adj[:, 2], -fwd[:, 0])
 
 
+def robust_rel(b, a, frac=1 / 500):
+    """rel_l2 over particles after dropping the worst fraction of them."""
+    e = np.linalg.norm((np.asarray(b, np.float64) - a).reshape(len(a), -1), axis=1)
+    keep = np.argsort(e)[:len(e) - int(len(e) * frac)]
+    return rel_l2(np.asarray(b)[keep], np.asarray(a)[keep])
+
+
 def test_nbody_adjoint_matches_oracle(cuda, nb_case):
     """Reversible adjoint: cotangents at the start, per-factor
     sensitivities and the Omega_m force term against the oracle's
-    nbody_adj (which itself matches float64 autograd)."""
+    nbody_adj (which itself matches float64 autograd).
+
+    The CIC weight gradient is piecewise constant, so a particle that float32
+    rounding puts on the other side of a cell boundary than the float64
+    oracle gets an O(1) different cotangent, which the remaining adjoint
+    steps spread to its neighbours.  Repeated runs of the 64^3-mesh case
+    show discrete outcomes: no such event (sensitivities within 1e-5..6e-5
+    of the oracle), or one of two events (cotangents 3.2e-4 / 1.3e-3,
+    sensitivities 5e-4 / 2e-3).  The cotangents are therefore compared
+    without the 0.2% of particles farthest off, and the particle sums
+    (sensitivities, Omega_m term) within 5e-3, which an error in the
+    adjoint itself exceeds by orders of magnitude."""
     oconf, gconf, pmid, disp, vel, ocos, gcos = nb_case
     rng = np.random.default_rng(11)
     dcot = rng.normal(size=disp.shape).astype(np.float32)
@@ -316,16 +334,18 @@ def test_nbody_adjoint_matches_oracle(cuda, nb_case):
     ptcl = pg.Particles(gconf, T(pmid, cuda), D, vel=V)
     out, _ = pg.nbody(ptcl, None, cos, gconf)
     ((out.disp * T(dcot, cuda)).sum() + (out.vel * T(vcot, cuda)).sum()).backward()
-    assert rel_l2(D.grad.cpu().numpy(), cot0.disp) < 1e-3
-    assert rel_l2(V.grad.cpu().numpy(), cot0.vel) < 1e-3
+    for got, want in ((D.grad, cot0.disp), (V.grad, cot0.vel)):
+        got = got.cpu().numpy()
+        assert robust_rel(got, want) < 1e-3, (robust_rel(got, want), rel_l2(got, want))
+        assert rel_l2(got, want) < 1e-2
 
     # explicit adjoint API: per-factor sensitivities and the Omega_m term
     ptcl1 = out.replace(disp=out.disp.detach(), vel=out.vel.detach(), acc=out.acc.detach())
     cot = pg.Particles(gconf, ptcl1.pmid, T(dcot, cuda), vel=T(vcot, cuda))
     p0, c0, fgrad, omg = gnb.nbody_adj(ptcl1, cot, None, gcos, gconf)
     ref = np.array([s for *_, s in sens['factors']])
-    assert rel_l2(fgrad.numpy(), ref) < 1e-3
-    assert abs(float(omg) / sens['Omega_m'] - 1) < 1e-3
+    assert rel_l2(fgrad.numpy(), ref) < 5e-3
+    assert abs(float(omg) / sens['Omega_m'] - 1) < 5e-3
     # the reconstructed initial state returns to the start
     assert rel_l2(p0.disp.cpu().numpy(), disp) < 1e-4
 
