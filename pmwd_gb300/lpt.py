@@ -171,11 +171,18 @@ class _LptGraph:
                 for _ in range(2):   # plans and allocator pools before capture
                     _lpt_device(self.modes, self.fac, self.kvec, self.disp0, self.vel0, conf)
             self.stream.synchronize()
+            # captured on this stream with stream-level syncs only (no device
+            # synchronize, which fails while another thread captures), in
+            # thread-local mode so other threads keep launching meanwhile
             self.graph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(self.graph, stream=self.stream,
-                                  capture_error_mode='thread_local'):
-                self.disp, self.vel = _lpt_device(self.modes, self.fac, self.kvec, self.disp0,
-                                                  self.vel0, conf)
+            with torch.cuda.stream(self.stream):
+                self.graph.capture_begin(capture_error_mode='thread_local')
+                try:
+                    self.disp, self.vel = _lpt_device(self.modes, self.fac, self.kvec,
+                                                      self.disp0, self.vel0, conf)
+                finally:
+                    self.graph.capture_end()
+            self.stream.synchronize()
 
     def run(self, modes, fac):
         cur = torch.cuda.current_stream(self.dev)
@@ -201,6 +208,9 @@ class _LptGraph:
         return out
 
 
+_BUILD_LOCK = threading.Lock()
+
+
 def _graph_for(conf, modes):
     key = (conf, modes.device.index)
     with _GRAPH_LOCK:
@@ -208,11 +218,15 @@ def _graph_for(conf, modes):
         if g is not None:
             _GRAPHS.move_to_end(key)
             return g
-    g = _LptGraph(conf, modes.device, tuple(modes.shape))
-    with _GRAPH_LOCK:
-        _GRAPHS[key] = g
-        while len(_GRAPHS) > _GRAPHS_MAX:
-            _GRAPHS.popitem(last=False)
+    with _BUILD_LOCK:   # one capture at a time; a racing caller finds it built
+        with _GRAPH_LOCK:
+            g = _GRAPHS.get(key)
+        if g is None:
+            g = _LptGraph(conf, modes.device, tuple(modes.shape))
+            with _GRAPH_LOCK:
+                _GRAPHS[key] = g
+                while len(_GRAPHS) > _GRAPHS_MAX:
+                    _GRAPHS.popitem(last=False)
     return g
 
 

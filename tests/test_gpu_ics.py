@@ -118,6 +118,35 @@ def test_lpt_graph_replay_matches_eager(cuda):
         assert rel_l2(g.vel.cpu().numpy(), e.vel.detach().cpu().numpy()) < 1e-6
 
 
+def test_lpt_graph_concurrent_callers(cuda):
+    """Host setup threads (as the server runs them) call lpt at once, each
+    needing its own graph: the captures are serialised, run on their own
+    streams, and every result equals the eager path's."""
+    import importlib
+    from concurrent.futures import ThreadPoolExecutor
+    glpt = importlib.import_module('pmwd_gb300.lpt')
+    glpt._GRAPHS.clear()
+    confs = [pg.Configuration(2.0, (s, s, s), m) for s in (16, 32) for m in (1, 2)]
+    cosmos = [pg.boltzmann(pg.SimpleLCDM(c), c) for c in confs]
+    modes = [pg.linear_modes(pg.white_noise(i, c, device=cuda), cos, c)
+             for i, (c, cos) in enumerate(zip(confs, cosmos))]
+    torch.cuda.synchronize()
+
+    def work(i):
+        with torch.no_grad():
+            p, _ = pg.lpt(modes[i], cosmos[i], confs[i])
+        torch.cuda.current_stream().synchronize()
+        return p.disp.cpu().numpy(), p.vel.cpu().numpy()
+
+    with ThreadPoolExecutor(4) as ex:
+        got = list(ex.map(work, list(range(len(confs))) * 2))
+    for i, c in enumerate(confs):
+        e, _ = pg.lpt(modes[i].clone().requires_grad_(True), cosmos[i], c)
+        for g in (got[i], got[i + len(confs)]):
+            assert rel_l2(g[0], e.disp.detach().cpu().numpy()) < 1e-6
+            assert rel_l2(g[1], e.vel.detach().cpu().numpy()) < 1e-6
+
+
 def test_lpt_statistics_match_published(cuda):
     """docs/examples/quickstart.ipynb prints, for 256^3 particles, spacing 1,
     2x mesh, SimpleLCDM, after 2LPT at a=1/64: disp.std() = 0.105 and
