@@ -8,6 +8,7 @@ from itertools import combinations, permutations
 
 import torch
 
+from . import _hostmath
 from .boltzmann import growth
 from .cosmology import E2
 from .gravity import laplace, neg_grad
@@ -236,10 +237,7 @@ def _wants_graph(modes, cosmo, conf):
     if modes.dtype != torch.complex64 or tuple(modes.shape) != tuple(
             conf.ptcl_grid_shape[:-1]) + (conf.ptcl_grid_shape[-1] // 2 + 1,):
         return False
-    if not torch.is_grad_enabled():
-        return True
-    return not (modes.requires_grad or any(
-        torch.is_tensor(v) and v.requires_grad for v in vars(cosmo).values()))
+    return not _hostmath.needs_grad(modes, cosmo)
 
 
 def lpt(modes, cosmo, conf):
@@ -259,8 +257,7 @@ def lpt(modes, cosmo, conf):
     if conf.lpt_order == 0:
         return Particles.gen_grid(conf, vel=True, device=dev), None
     if _wants_graph(modes, cosmo, conf):
-        with torch.no_grad():
-            fac = _growth_factors(cosmo, conf)
+        fac = torch.from_numpy(_hostmath.lpt_factors(cosmo, conf))
         pmid, disp, vel = _graph_for(conf, modes).run(modes, fac)
         return Particles(conf, pmid, disp, vel=vel), None
     fac = _growth_factors(cosmo, conf).to(dev)

@@ -11,6 +11,7 @@ import math
 import numpy as np
 import torch
 
+from . import _hostmath
 from .boltzmann import linear_power
 from .pm_util import fftfreq, fftfwd, fftinv
 
@@ -85,12 +86,21 @@ def linear_modes(modes, cosmo, conf, a=None, real=False):
     mi = _mode_index(conf.ptcl_grid_shape, dev)
     if mi is not None:
         # the table is small (dim D / 4 + 1 entries): evaluated on the host,
-        # where the cosmology's tables and parameters live, then gathered
+        # where the cosmology's tables and parameters live, then gathered;
+        # in NumPy when no gradient is needed
         m, D, mmax = mi
-        mv = torch.arange(mmax + 1, dtype=torch.float64)
-        k = (2 * math.pi / conf.ptcl_spacing) * torch.sqrt(mv / D)
-        Plin = linear_power(k, a, cosmo, conf).to(torch.float32)
-        amp = _SafeSqrt.apply(Plin * conf.box_vol).to(dev)[m]
+        # NumPy is faster for small tables (no per-op dispatch), torch's
+        # threaded CPU ops for large ones (197K entries at 512^3)
+        if mmax < (1 << 16) and not _hostmath.needs_grad(modes, cosmo, a):
+            kn = (2 * math.pi / conf.ptcl_spacing) * np.sqrt(np.arange(mmax + 1) / D)
+            an = None if a is None else float(a)
+            tab = torch.from_numpy(_hostmath.mode_amplitude(kn, an, cosmo, conf))
+        else:
+            mv = torch.arange(mmax + 1, dtype=torch.float64)
+            k = (2 * math.pi / conf.ptcl_spacing) * torch.sqrt(mv / D)
+            Plin = linear_power(k, a, cosmo, conf).to(torch.float32)
+            tab = _SafeSqrt.apply(Plin * conf.box_vol)
+        amp = tab.to(dev)[m]
     else:
         kvec = fftfreq(conf.ptcl_grid_shape, conf.ptcl_spacing, dtype=torch.float32, device=dev)
         k = torch.sqrt(sum(kk ** 2 for kk in kvec))
