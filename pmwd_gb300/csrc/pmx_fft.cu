@@ -30,6 +30,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <cstdlib>
 #include <string>
 #include <utility>
@@ -551,9 +553,24 @@ int launch_xpass(bool adj, const float2 *in, float2 *out, const float *kt, const
     const int T = adj ? XCfg<N, XTA>::T : XCfg<N, XTF>::T;
     g.ncol_tiles = (n2h + T - 1) / T + 1;
     g.align = (n1 * rs) % 4 == 0;
-    PMX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    // the shared-memory opt-in and the occupancy query once per device and
+    // kernel: a small mesh's force is short enough for them to show
     int per_sm = 0;
-    PMX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, sm));
+    {
+        static std::mutex mu;
+        static std::map<std::pair<int, bool>, int> known;
+        int dev = 0;
+        PMX_CUDA(cudaGetDevice(&dev));
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = known.find({dev, adj});
+        if (it != known.end()) {
+            per_sm = it->second;
+        } else {
+            PMX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            PMX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, sm));
+            known[{dev, adj}] = per_sm;
+        }
+    }
     if (per_sm < 1) return fail(PMX_ERR_CUDA, "x-pass kernel does not fit on an SM");
     const int64_t tiles = n1 * g.ncol_tiles;
     const int64_t cap = (int64_t)device_sms() * per_sm;

@@ -7,6 +7,8 @@ differ from the reference's while the distribution is the same.
 """
 
 import math
+import threading
+from collections import OrderedDict
 
 import numpy as np
 import torch
@@ -45,14 +47,22 @@ class _SafeSqrt(torch.autograd.Function):
                            torch.zeros_like(g))
 
 
-_MODE_INDEX = {}
+_MODE_INDEX = OrderedDict()   # (shape, device) -> index; the 4 most recent
+_MODE_LOCK = threading.Lock()
 
 
 def _mode_index(shape, device):
     key = (tuple(shape), str(device))
-    if key not in _MODE_INDEX:
-        _MODE_INDEX[key] = _mode_index_build(shape, device)
-    return _MODE_INDEX[key]
+    with _MODE_LOCK:
+        if key in _MODE_INDEX:
+            _MODE_INDEX.move_to_end(key)
+            return _MODE_INDEX[key]
+    val = _mode_index_build(shape, device)
+    with _MODE_LOCK:
+        _MODE_INDEX[key] = val
+        while len(_MODE_INDEX) > 4:
+            _MODE_INDEX.popitem(last=False)
+    return val
 
 
 def _mode_index_build(shape, device):
