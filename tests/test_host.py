@@ -131,3 +131,28 @@ def test_factor_gradient_wrt_cosmology(both):
         c = oc.with_tables(oc.simple_lcdm(Omega_m=0.3 + s * h), oconf)
         fd.append(oc.kick_factor(*args, c, oconf))
     np.testing.assert_allclose(float(Om.grad), (fd[0] - fd[1]) / (2 * h), rtol=1e-5)
+
+
+@pytest.mark.parametrize('pars', [dict(), dict(Omega_m=0.25, Omega_k_=0.05, w_0_=-0.9, w_a_=0.1)])
+def test_host_math_matches_torch_path(pars):
+    """The NumPy evaluation used by calls without gradients (amplitude table
+    of linear_modes, 2LPT growth factors) against the torch code it mirrors:
+    the same float32 factors, and amplitudes within one float32 ulp."""
+    import math
+    hm = importlib.import_module('pmwd_gb300._hostmath')
+    glpt = importlib.import_module('pmwd_gb300.lpt')
+    conf = pg.Configuration(2.0, (16, 32, 8), 2)
+    cos = pg.SimpleLCDM(conf).replace(**{k: torch.tensor(v, dtype=torch.float64)
+                                         for k, v in pars.items()})
+    cos = pg.boltzmann(cos, conf)
+    np.testing.assert_array_equal(hm.lpt_factors(cos, conf), glpt._growth_factors(cos, conf).numpy())
+    m = np.arange(0, 3 * 32 * 32 // 4 + 1)
+    k = (2 * math.pi / conf.ptcl_spacing) * np.sqrt(m / 32 ** 2)
+    amp_np = hm.mode_amplitude(k, 0.5, cos, conf)
+    P = pg.linear_power(torch.from_numpy(k), 0.5, cos, conf).to(torch.float32)
+    amp_t = torch.sqrt(P * conf.box_vol).numpy()
+    np.testing.assert_allclose(amp_np, amp_t, rtol=2.5e-7, atol=0)
+    assert not hm.needs_grad(torch.zeros(2), cos)
+    assert hm.needs_grad(torch.zeros(2, requires_grad=True))
+    with torch.no_grad():
+        assert not hm.needs_grad(torch.zeros(2, requires_grad=True))
