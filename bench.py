@@ -22,7 +22,6 @@ shard); value = total particle-steps of all ranks / max-over-ranks time.
 import argparse
 import ctypes
 import json
-import math
 import os
 import statistics
 import subprocess

@@ -21,7 +21,6 @@ import numpy as np
 import torch
 
 from . import _lib
-from .cosmology import E2, H_deriv, Omega_m_a
 
 DT = torch.float64
 

@@ -15,7 +15,6 @@ import math
 import torch
 
 from . import _lib
-from .pm_util import fftfreq
 from .scatter import _check_ptcl
 
 
