@@ -284,6 +284,16 @@ int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
                     int32_t nedges, int32_t right, int32_t nbin, double deconv,
                     double *ksum, double *psum, double *nsum, void *stream);
 
+/* pmx_powspec_bin for spectra stored half-axis major, (n2/2+1, n0, n1) per
+ * batch element with the y axis contiguous -- the layout torch's CUDA rfftn
+ * returns for (n0, n1, n2/2+1) -- read in place instead of transposed.
+ * Power-of-two grids up to 2048 only. */
+int pmx_powspec_bin_zmajor(const float *F, const float *G, int64_t nbatch,
+                           const int64_t grid_shape[3], const double *kx,
+                           const double *ky, const double *kz, const double *edges,
+                           int32_t nedges, int32_t right, int32_t nbin, double deconv,
+                           double *ksum, double *psum, double *nsum, void *stream);
+
 /* --------------------------------------------------------------------------
  * Growth functions (host)
  * ------------------------------------------------------------------------ */

@@ -67,6 +67,8 @@ SIGNATURES = {
                                     c_p, c_i64, c_i64, c_i32, c_p, c_d, c_p, c_p]),
     'pmx_powspec_bin': (c_int, [c_p, c_p, c_i64, ctypes.POINTER(c_i64), c_p, c_p, c_p, c_p, c_i32,
                                 c_i32, c_i32, c_d, c_p, c_p, c_p, c_p]),
+    'pmx_powspec_bin_zmajor': (c_int, [c_p, c_p, c_i64, ctypes.POINTER(c_i64), c_p, c_p, c_p, c_p,
+                                       c_i32, c_i32, c_i32, c_d, c_p, c_p, c_p, c_p]),
     'pmx_growth_ode': (c_int, [c_p, c_i64, c_p, c_i64, c_d, c_d, c_p, c_p]),
     'pmx_profile_enable': (c_int, [c_p, c_int]),
     'pmx_profile_read': (c_int, [c_p, ctypes.POINTER(c_d), ctypes.POINTER(c_i64),

@@ -171,6 +171,7 @@ struct Pow2Args {
     const int *btab;               // bin(m), nbin = none
     const float *wx, *wy, *wz;     // sinc^-deconv per axis, or NULL
     int nbin;
+    int zm;                        // 1: layout (n2h, n0, n1), y contiguous
     double *ksum, *psum, *nsum;
 };
 
@@ -203,7 +204,7 @@ __device__ __forceinline__ float warp_sumf(float v) {
 constexpr int PRIV_BINS = 64;
 
 template <bool CROSS, bool GEOM, bool WIN, bool PRIV>
-__global__ void __launch_bounds__(ST) k_powspec_rows(Pow2Args a) {
+__global__ void __launch_bounds__(ST, 6) k_powspec_rows(Pow2Args a) {
     extern __shared__ double sbase[];  // 4 doubles per bin (per warp with PRIV)
     const int nacc = (PRIV ? ST / 32 : 1) * 4 * a.nbin;
     for (int i = threadIdx.x; i < nacc; i += ST) sbase[i] = 0.0;
@@ -211,29 +212,52 @@ __global__ void __launch_bounds__(ST) k_powspec_rows(Pow2Args a) {
     const int lane = threadIdx.x & 31;
     double *sb = PRIV ? sbase + (threadIdx.x >> 5) * 4 * a.nbin : sbase;
     const int n2h = (int)a.n2h, az = (int)a.az;
-    const int64_t nrows = a.n0 * a.n1;
+    // rows of contiguous cells: (x, y) rows along kz, or with zm (kz, x)
+    // rows along y (the layout torch's CUDA rfftn returns)
+    const int64_t nrows = a.zm ? a.n2h * a.n0 : a.n0 * a.n1;
+    const int nlane = a.zm ? (int)a.n1 : n2h;
     const int64_t wstride = (int64_t)gridDim.x * (ST / 32);
     for (int64_t row = blockIdx.x * (int64_t)(ST / 32) + (threadIdx.x >> 5); row < nrows;
          row += wstride) {  // warp-uniform
-        const int64_t i = row / a.n1, j = row - i * a.n1;
-        const int64_t si = signed_idx(i, a.h0), sj = signed_idx(j, a.h1);
-        const int mrow = (int)(si * si * a.ax + sj * sj * a.ay);
-        const float wxy = WIN ? a.wx[i] * a.wy[j] : 1.f;
-        const float2 *Fr = a.F + row * a.n2h;
-        const float2 *Gr = CROSS ? a.G + row * a.n2h : nullptr;
-        for (int l0 = 0; l0 < n2h; l0 += 32) {
-            const int l = l0 + lane;
+        int64_t i, j = 0, lr = 0;
+        int mrow;
+        if (a.zm) {
+            lr = row / a.n0;
+            i = row - lr * a.n0;
+            const int64_t si = signed_idx(i, a.h0);
+            mrow = (int)(si * si * a.ax + lr * lr * a.az);
+        } else {
+            i = row / a.n1;
+            j = row - i * a.n1;
+            const int64_t si = signed_idx(i, a.h0), sj = signed_idx(j, a.h1);
+            mrow = (int)(si * si * a.ax + sj * sj * a.ay);
+        }
+        const float2 *Fr = a.F + row * nlane;
+        const float2 *Gr = CROSS ? a.G + row * nlane : nullptr;
+        for (int c0 = 0; c0 < nlane; c0 += 32) {
+            const int c = c0 + lane;   // kz, or y with zm
             int b = a.nbin;
             float pr = 0.f, pi = 0.f;
             double kn = 0.0, nn = 0.0;
-            if (l < n2h) {
-                const int m = mrow + l * l * az;
+            if (c < nlane) {
+                int m, l;
+                int64_t jj;
+                if (a.zm) {
+                    const int64_t sjj = signed_idx(c, a.h1);
+                    m = mrow + (int)(sjj * sjj * a.ay);
+                    l = (int)lr;
+                    jj = c;
+                } else {
+                    m = mrow + c * c * az;
+                    l = c;
+                    jj = j;
+                }
                 b = a.btab[m];
                 if (b < a.nbin) {
                     for (int64_t t = 0; t < a.nb; ++t) {
-                        const float2 f = Fr[t * a.Mc + l];
+                        const float2 f = Fr[t * a.Mc + c];
                         if (CROSS) {
-                            const float2 gg = Gr[t * a.Mc + l];
+                            const float2 gg = Gr[t * a.Mc + c];
                             pr += __fadd_rn(__fmul_rn(f.x, gg.x), __fmul_rn(f.y, gg.y));
                             pi += __fsub_rn(__fmul_rn(f.y, gg.x), __fmul_rn(f.x, gg.y));
                         } else {
@@ -241,7 +265,7 @@ __global__ void __launch_bounds__(ST) k_powspec_rows(Pow2Args a) {
                         }
                     }
                     if (WIN) {  // ((P wx) wy) wz
-                        const float w = wxy * a.wz[l];
+                        const float w = (a.wx[i] * a.wy[jj]) * a.wz[l];
                         pr *= w;
                         pi *= w;
                     }
@@ -366,11 +390,10 @@ __global__ void k_sinc_tab(const double *k, int64_t n, double deconv, float *w) 
 
 using namespace pmx;
 
-extern "C" int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
-                               const int64_t grid_shape[3], const double *kx, const double *ky,
-                               const double *kz, const double *edges, int32_t nedges,
-                               int32_t right, int32_t nbin, double deconv, double *ksum,
-                               double *psum, double *nsum, void *stream) {
+static int powspec_bin(const float *F, const float *G, int64_t nbatch, const int64_t grid_shape[3],
+                       const double *kx, const double *ky, const double *kz, const double *edges,
+                       int32_t nedges, int32_t right, int32_t nbin, double deconv, double *ksum,
+                       double *psum, double *nsum, void *stream, bool zm) {
     clear_error();
     if (!F || !grid_shape || !kx || !ky || !kz || !edges || !psum)
         return fail(PMX_ERR_ARG, "null argument");
@@ -406,6 +429,7 @@ extern "C" int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
         // tables of k(m), bin(m) and the per-axis windows: stream-ordered
         // scratch, freed after the launch (the stream keeps them alive)
         Pow2Args p;
+        p.zm = zm;
         p.F = a.F;
         p.G = a.G;
         p.nb = a.nb;
@@ -457,6 +481,7 @@ extern "C" int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
         PMX_CUDA(cudaFreeAsync(scr, s));
         return PMX_OK;
     }
+    if (zm) return fail(PMX_ERR_SHAPE, "the (n2h, n0, n1) layout needs a power-of-two grid <= 2048");
     if (!ksum) return fail(PMX_ERR_ARG, "ksum/nsum may be NULL only for power-of-two grids <= 2048");
     const int grid = stride_grid(a.Mc, ST, 4);
     if (nbin <= SMEM_BINS) {
@@ -467,4 +492,22 @@ extern "C" int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
     }
     PMX_LAUNCH_CHECK("k_powspec");
     return PMX_OK;
+}
+
+extern "C" int pmx_powspec_bin(const float *F, const float *G, int64_t nbatch,
+                               const int64_t grid_shape[3], const double *kx, const double *ky,
+                               const double *kz, const double *edges, int32_t nedges,
+                               int32_t right, int32_t nbin, double deconv, double *ksum,
+                               double *psum, double *nsum, void *stream) {
+    return powspec_bin(F, G, nbatch, grid_shape, kx, ky, kz, edges, nedges, right, nbin, deconv,
+                       ksum, psum, nsum, stream, false);
+}
+
+extern "C" int pmx_powspec_bin_zmajor(const float *F, const float *G, int64_t nbatch,
+                                      const int64_t grid_shape[3], const double *kx,
+                                      const double *ky, const double *kz, const double *edges,
+                                      int32_t nedges, int32_t right, int32_t nbin, double deconv,
+                                      double *ksum, double *psum, double *nsum, void *stream) {
+    return powspec_bin(F, G, nbatch, grid_shape, kx, ky, kz, edges, nedges, right, nbin, deconv,
+                       ksum, psum, nsum, stream, true);
 }

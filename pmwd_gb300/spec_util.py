@@ -92,11 +92,21 @@ def _bin_cuda(F, G, grid_shape, edges, right, bnum, deconv):
     from . import _lib
     dev = F.device
     nb = math.prod(F.shape[:-3])
-    F = F.contiguous()
     if G is not None:
-        G = G.to(torch.complex64).contiguous()
+        G = G.to(torch.complex64)
         if G.shape != F.shape:
             raise ValueError(f'shape mismatch: {G.shape} != {F.shape}')
+    # torch's CUDA rfftn returns (..., n0, n1, n2h) stored half-axis major,
+    # (..., n2h, n0, n1) contiguous: bin it in place instead of transposing
+    zm = (_pow2_grid(grid_shape) and bnum <= 2048
+          and not F.is_contiguous() and F.movedim(-1, -3).is_contiguous()
+          and (G is None or (G.stride() == F.stride())))
+    if zm:
+        F = F.movedim(-1, -3)
+        G = None if G is None else G.movedim(-1, -3)
+    else:
+        F = F.contiguous()
+        G = None if G is None else G.contiguous()
     kx, ky, kz = (k.reshape(-1).contiguous() for k in
                   fftfreq(grid_shape, None, dtype=torch.float64, device=dev))
     e = edges.to(device=dev, dtype=torch.float64).contiguous()
@@ -111,7 +121,8 @@ def _bin_cuda(F, G, grid_shape, edges, right, bnum, deconv):
     else:
         ksum = nsum = None
     shape = (_lib.c_i64 * 3)(*grid_shape)
-    _lib.call('pmx_powspec_bin', torch.view_as_real(F), None if G is None else torch.view_as_real(G),
+    _lib.call('pmx_powspec_bin_zmajor' if zm else 'pmx_powspec_bin', torch.view_as_real(F),
+              None if G is None else torch.view_as_real(G),
               nb, shape, kx, ky, kz, e, len(e), int(right), bnum, float(deconv or 0.0), ksum, psum,
               nsum, _lib.stream_ptr(dev))
     if cached is None:

@@ -73,6 +73,31 @@ def test_powspec_kernel_matches_oracle(cuda, shape, bins):
     np.testing.assert_allclose(b_g.cpu().numpy(), b_o, rtol=1e-12)
 
 
+@pytest.mark.parametrize('shape, bins', [((32, 64, 16), 1j / 3), ((64, 32, 32), 0.5),
+                                         ((2, 16, 32, 8), 2)])
+def test_powspec_half_axis_major_layout(cuda, shape, bins):
+    """torch's CUDA rfftn stores (n0, n1, n2h) half-axis major; the kernel
+    bins that layout in place (pmx_powspec_bin_zmajor) and must give the
+    sums of the transposed, contiguous copy (pmx_powspec_bin), also for a
+    cross spectrum and a leading batch axis."""
+    from pmwd_gb300 import spec_util as su
+    rng = np.random.default_rng(7)
+    f = torch.from_numpy(rng.normal(size=shape).astype(np.float32)).to(cuda)
+    g = torch.from_numpy(rng.normal(size=shape).astype(np.float32)).to(cuda)
+    F, G = su.fftfwd(f, axes=(-3, -2, -1)), su.fftfwd(g, axes=(-3, -2, -1))
+    grid = tuple(shape[-3:])
+    bnum, bcut, edges, right = su._getbins(grid, bins, True)
+    for GG in (None, G):
+        su._GEOMETRY.clear()
+        k1, P1, N1 = su._bin_cuda(F, GG, grid, edges, right, bnum, None)
+        su._GEOMETRY.clear()
+        k2, P2, N2 = su._bin_cuda(F.contiguous(), None if GG is None else GG.contiguous(), grid,
+                                  edges, right, bnum, None)
+        np.testing.assert_allclose(k1.cpu().numpy(), k2.cpu().numpy(), rtol=1e-12)
+        np.testing.assert_array_equal(N1.cpu().numpy(), N2.cpu().numpy())
+        np.testing.assert_allclose(P1.cpu().numpy(), P2.cpu().numpy(), rtol=1e-5)
+
+
 @pytest.mark.parametrize('shape', [(2, 16, 18, 20), (2, 16, 32, 8)])
 def test_powspec_kernel_cross_deconv_batch(cuda, shape):
     """Cross spectrum with a leading channel axis, CIC deconvolution and
