@@ -65,6 +65,8 @@ def parse():
     ap.add_argument('--gradient', action='store_true',
                     help="the reference quickstart's gradient: 256^3 / 512^3 mesh, 63 steps, "
                          "d var(dens - target) / d(modes, cosmology)")
+    ap.add_argument('--powspec', type=int, default=0,
+                    help='power-spectrum binning of an N^3 field (rfftn + pmx_powspec_bin)')
     ap.add_argument('--published', action='store_true',
                     help="pmwd's own timing table (perf.py): growth, 2LPT and N-body per step "
                          "for ptcl grids 32^3..512^3 at mesh x1 and x2")
@@ -764,6 +766,43 @@ def run_gradient(args):
     print(json.dumps(line), flush=True)
 
 
+def run_powspec(args):
+    """Power spectrum of an n^3 Gaussian field (spec_util.py:50-147): torch's
+    rfftn (cuFFT), then the binning pass (pmx_powspec_bin*) for pmwd's
+    default log bins (1j/3) and for unit linear bins, each after a call
+    that caches the grid's k and N sums; CUDA events, mean of 5 calls."""
+    import torch
+    from pmwd_gb300 import spec_util
+    torch.cuda.set_device(0)
+    dev = torch.device('cuda', 0)
+    n = args.powspec
+    grid = (n, n, n)
+    f = torch.randn(grid, device=dev, generator=torch.Generator(device=dev).manual_seed(0))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    F = spec_util.fftfwd(f, axes=(-3, -2, -1))
+    out = {'rfftn_ms': timed(lambda: spec_util.fftfwd(f, axes=(-3, -2, -1)))}
+    for name, bins in (('log_1j/3', 1j / 3), ('linear_unit', 1.0)):
+        bnum, _, edges, right = spec_util._getbins(grid, bins, True)
+        out[name] = {'bins': bnum, 'binning_ms': timed(
+            lambda: spec_util._bin_cuda(F, None, grid, edges, right, bnum, None)),
+            'spectrum_gb': F.numel() * 8 / 1e9}
+        out[name]['gbs'] = out[name]['spectrum_gb'] / out[name]['binning_ms'] * 1e3
+    print(json.dumps({'metric': 'power spectrum binning', 'unit': 'ms',
+                      'config': {'workload': f'{n}^3 Gaussian field, complex64 half spectrum'},
+                      **out}), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get('RANK', 0))
@@ -787,6 +826,10 @@ def main():
     if args.gradient:
         if rank == 0:
             run_gradient(args)
+        return
+    if args.powspec:
+        if rank == 0:
+            run_powspec(args)
         return
     if world > 1:
         import torch
