@@ -186,8 +186,6 @@ __global__ void k_pow2_tables(int64_t mmax, double D, const double *edges, int n
     }
 }
 
-__device__ __forceinline__ int64_t signed_idx(int64_t i, int64_t n) { return i <= n / 2 ? i : i - n; }
-
 __device__ __forceinline__ float warp_sumf(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -214,38 +212,40 @@ __global__ void __launch_bounds__(ST, 6) k_powspec_rows(Pow2Args a) {
     const int n2h = (int)a.n2h, az = (int)a.az;
     // rows of contiguous cells: (x, y) rows along kz, or with zm (kz, x)
     // rows along y (the layout torch's CUDA rfftn returns)
-    const int64_t nrows = a.zm ? a.n2h * a.n0 : a.n0 * a.n1;
-    const int nlane = a.zm ? (int)a.n1 : n2h;
-    const int64_t wstride = (int64_t)gridDim.x * (ST / 32);
-    for (int64_t row = blockIdx.x * (int64_t)(ST / 32) + (threadIdx.x >> 5); row < nrows;
+    // every index below fits in 32 bits (grids up to 2048: rows < 2^22,
+    // bin-table indices < 2^31)
+    const int n0 = (int)a.n0, n1 = (int)a.n1, h0 = a.h0, h1 = a.h1;
+    const int ax = (int)a.ax, ay = (int)a.ay;
+    const int nrows = a.zm ? n2h * n0 : n0 * n1;
+    const int nlane = a.zm ? n1 : n2h;
+    const int wstride = gridDim.x * (ST / 32);
+    for (int row = blockIdx.x * (ST / 32) + (threadIdx.x >> 5); row < nrows;
          row += wstride) {  // warp-uniform
-        int64_t i, j = 0, lr = 0;
-        int mrow;
+        int i, j = 0, lr = 0, mrow;
         if (a.zm) {
-            lr = row / a.n0;
-            i = row - lr * a.n0;
-            const int64_t si = signed_idx(i, a.h0);
-            mrow = (int)(si * si * a.ax + lr * lr * a.az);
+            lr = row / n0;
+            i = row - lr * n0;
+            const int si = i <= h0 / 2 ? i : i - h0;
+            mrow = si * si * ax + lr * lr * az;
         } else {
-            i = row / a.n1;
-            j = row - i * a.n1;
-            const int64_t si = signed_idx(i, a.h0), sj = signed_idx(j, a.h1);
-            mrow = (int)(si * si * a.ax + sj * sj * a.ay);
+            i = row / n1;
+            j = row - i * n1;
+            const int si = i <= h0 / 2 ? i : i - h0, sj = j <= h1 / 2 ? j : j - h1;
+            mrow = si * si * ax + sj * sj * ay;
         }
-        const float2 *Fr = a.F + row * nlane;
-        const float2 *Gr = CROSS ? a.G + row * nlane : nullptr;
+        const float2 *Fr = a.F + (int64_t)row * nlane;
+        const float2 *Gr = CROSS ? a.G + (int64_t)row * nlane : nullptr;
         for (int c0 = 0; c0 < nlane; c0 += 32) {
             const int c = c0 + lane;   // kz, or y with zm
             int b = a.nbin;
             float pr = 0.f, pi = 0.f;
             double kn = 0.0, nn = 0.0;
             if (c < nlane) {
-                int m, l;
-                int64_t jj;
+                int m, l, jj;
                 if (a.zm) {
-                    const int64_t sjj = signed_idx(c, a.h1);
-                    m = mrow + (int)(sjj * sjj * a.ay);
-                    l = (int)lr;
+                    const int sjj = c <= h1 / 2 ? c : c - h1;
+                    m = mrow + sjj * sjj * ay;
+                    l = lr;
                     jj = c;
                 } else {
                     m = mrow + c * c * az;
