@@ -149,6 +149,7 @@ def powspec(f, spacing, bins=1j / 3, cut_zero=True, cut_nyq=True):
     NN = np.bincount(b, weights=N.ravel(), minlength=bnum)[:bnum]
     sl = slice(int(cut_zero), bcut)
     kk, PP, NN, edges = kk[sl], PP[sl], NN[sl], edges[:bcut]
-    kk = kk / NN * 2 * math.pi / spacing
-    PP = PP / NN * spacing ** 3 / math.prod(grid_shape)
+    with np.errstate(invalid='ignore', divide='ignore'):   # empty bins: NaN, as the reference
+        kk = kk / NN * 2 * math.pi / spacing
+        PP = PP / NN * spacing ** 3 / math.prod(grid_shape)
     return kk, PP, NN, edges * 2 * math.pi / spacing
