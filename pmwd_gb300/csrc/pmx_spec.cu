@@ -348,6 +348,128 @@ __global__ void __launch_bounds__(ST, 6) k_powspec_rows(Pow2Args a) {
     }
 }
 
+// Half-axis-major spectra with n1 a multiple of 32: the warp takes row
+// (kz, x) and lane r walks the contiguous run y in [r n1/32, (r+1) n1/32),
+// keeping the sums of its current bin in registers.  The bins are shells in
+// |k|, so a run changes bin rarely: then the lane adds its sums to the bin
+// array, and at the end of the row the lanes holding the same bin are
+// merged by shuffles and added once.  Every shared-memory add is atomic.
+template <bool CROSS, bool GEOM, bool WIN, bool PRIV>
+__global__ void __launch_bounds__(ST, 6) k_powspec_runs(Pow2Args a) {
+    extern __shared__ double sbase[];  // 4 doubles per bin (per warp with PRIV)
+    const int nacc = (PRIV ? ST / 32 : 1) * 4 * a.nbin;
+    for (int i = threadIdx.x; i < nacc; i += ST) sbase[i] = 0.0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    double *sb = PRIV ? sbase + (threadIdx.x >> 5) * 4 * a.nbin : sbase;
+    const int n2h = (int)a.n2h, n0 = (int)a.n0, n1 = (int)a.n1, h0 = a.h0, h1 = a.h1;
+    const int ax = (int)a.ax, ay = (int)a.ay, az = (int)a.az, nbin = a.nbin;
+    const int R = n1 / 32, nrows = n2h * n0;
+    const int wstride = gridDim.x * (ST / 32);
+    auto add = [&](int b, float pr, float pi, double kn, double nn) {
+        atomicAdd(sb + 4 * b + 1, (double)pr);
+        if (CROSS) atomicAdd(sb + 4 * b + 2, (double)pi);
+        if (GEOM) {
+            atomicAdd(sb + 4 * b, kn);
+            atomicAdd(sb + 4 * b + 3, nn);
+        }
+    };
+    for (int row = blockIdx.x * (ST / 32) + (threadIdx.x >> 5); row < nrows;
+         row += wstride) {  // warp-uniform
+        const int l = row / n0, i = row - l * n0;
+        const int si = i <= h0 / 2 ? i : i - h0;
+        const int mrow = si * si * ax + l * l * az;
+        const bool two = !(l == 0 || (a.nyq_z && l == n2h - 1));
+        const int j0 = lane * R;
+        const float2 *Fr = a.F + (int64_t)row * n1 + j0;
+        const float2 *Gr = CROSS ? a.G + (int64_t)row * n1 + j0 : nullptr;
+        int cur = nbin;
+        float ar = 0.f, ai = 0.f;
+        double ak = 0.0, an = 0.0;
+        for (int r = 0; r < R; ++r) {
+            const int j = j0 + r;
+            const int sj = j <= h1 / 2 ? j : j - h1;
+            const int m = mrow + sj * sj * ay;
+            const int b = a.btab[m];
+            if (b != cur) {
+                if (cur < nbin) add(cur, ar, ai, ak, an);
+                cur = b;
+                ar = ai = 0.f;
+                ak = an = 0.0;
+            }
+            if (b < nbin) {
+                float pr = 0.f, pi = 0.f;
+                for (int64_t t = 0; t < a.nb; ++t) {
+                    const float2 f = Fr[t * a.Mc + r];
+                    if (CROSS) {
+                        const float2 gg = Gr[t * a.Mc + r];
+                        pr += __fadd_rn(__fmul_rn(f.x, gg.x), __fmul_rn(f.y, gg.y));
+                        pi += __fsub_rn(__fmul_rn(f.y, gg.x), __fmul_rn(f.x, gg.y));
+                    } else {
+                        pr += fmaf(f.x, f.x, f.y * f.y);
+                    }
+                }
+                if (WIN) {  // ((P wx) wy) wz
+                    const float w = (a.wx[i] * a.wy[j]) * a.wz[l];
+                    pr *= w;
+                    pi *= w;
+                }
+                if (two) {
+                    pr += pr;
+                    pi += pi;
+                }
+                ar += pr;
+                ai += pi;
+                if (GEOM) {
+                    const double k = a.ktab[m];
+                    ak += two ? k + k : k;
+                    an += two ? 2.0 : 1.0;
+                }
+            }
+        }
+        __syncwarp();
+        // end of row: lanes still holding sums merge per bin
+        const int b = cur;
+        const unsigned peers = __match_any_sync(0xffffffffu, b);
+        const int ndist = __popc(__ballot_sync(0xffffffffu, lane == __ffs(peers) - 1));
+        if (ndist > 4) {
+            if (b < nbin) add(b, ar, ai, ak, an);
+        } else {
+            unsigned pending = __ballot_sync(0xffffffffu, b < nbin);
+            while (pending) {
+                const int src = __ffs(pending) - 1;
+                const int bb = __shfl_sync(0xffffffffu, b, src);
+                const bool mine = b == bb;
+                const float spr = warp_sumf(mine ? ar : 0.f);
+                const float spi = CROSS ? warp_sumf(mine ? ai : 0.f) : 0.f;
+                double sk = 0.0, sn = 0.0;
+                if (GEOM) {
+                    sk = warp_sum(mine ? ak : 0.0);
+                    sn = warp_sum(mine ? an : 0.0);
+                }
+                if (lane == src) add(bb, spr, spi, sk, sn);
+                pending &= ~__ballot_sync(0xffffffffu, mine);
+            }
+        }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < a.nbin; b += ST) {
+        double acc[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[c] = sbase[4 * b + c];
+        if (PRIV)
+            for (int w = 1; w < ST / 32; ++w)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[c] += sbase[w * 4 * a.nbin + 4 * b + c];
+        if (GEOM) {
+            atomicAdd(a.ksum + b, acc[0]);
+            atomicAdd(a.nsum + b, acc[3]);
+        }
+        atomicAdd(a.psum + 2 * b, acc[1]);
+        if (CROSS) atomicAdd(a.psum + 2 * b + 1, acc[2]);
+    }
+}
+
 // Dynamic shared memory above the default 48 KB needs the opt-in attribute.
 template <class K>
 void allow_smem(K *kern, size_t sm) {
@@ -359,6 +481,17 @@ void allow_smem(K *kern, size_t sm) {
 template <bool CROSS, bool GEOM, bool PRIV>
 void launch_rows_p(const Pow2Args &p, cudaStream_t s) {
     const size_t sm = (PRIV ? ST / 32 : 1) * 4 * (size_t)p.nbin * sizeof(double);
+    if (p.zm && p.n1 >= 32 && p.n1 % 32 == 0) {   // contiguous runs per lane
+        const int grid = stride_grid(p.n2h * p.n0 * 32, ST, 6);
+        if (p.wx) {
+            allow_smem(k_powspec_runs<CROSS, GEOM, true, PRIV>, sm);
+            k_powspec_runs<CROSS, GEOM, true, PRIV><<<grid, ST, sm, s>>>(p);
+        } else {
+            allow_smem(k_powspec_runs<CROSS, GEOM, false, PRIV>, sm);
+            k_powspec_runs<CROSS, GEOM, false, PRIV><<<grid, ST, sm, s>>>(p);
+        }
+        return;
+    }
     const int grid = stride_grid(p.n0 * p.n1 * 32, ST, 8);
     if (p.wx) {
         allow_smem(k_powspec_rows<CROSS, GEOM, true, PRIV>, sm);
