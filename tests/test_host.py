@@ -156,3 +156,19 @@ def test_host_math_matches_torch_path(pars):
     assert hm.needs_grad(torch.zeros(2, requires_grad=True))
     with torch.no_grad():
         assert not hm.needs_grad(torch.zeros(2, requires_grad=True))
+
+
+def test_growth_ode_einstein_de_sitter_is_exact():
+    """Omega_m = 1: D_1 = a and D_2 = -3/7 a^2 exactly, so the integrated
+    state (G1, G1', G2, G2') stays (1, 0, 3/7, 0) at every output point."""
+    import ctypes
+    from pmwd_gb300 import _lib
+    lib = _lib.load()
+    prm = np.array([1.0, 0.0, -1.0, 0.0])
+    lna = np.linspace(np.log(1e-5), 0.0, 40)
+    y = np.empty((40, 1, 4))
+    dy = np.empty((40, 1, 4))
+    f = lambda x: x.ctypes.data_as(ctypes.c_void_p)
+    assert lib.pmx_growth_ode(f(prm), 1, f(lna), 40, 1e-11, 1e-13, f(y), f(dy)) == 0
+    np.testing.assert_allclose(y[:, 0, :], np.tile([1.0, 0.0, 3 / 7, 0.0], (40, 1)), atol=1e-12)
+    np.testing.assert_allclose(dy[:, 0, :], 0.0, atol=1e-12)
