@@ -210,8 +210,10 @@ __global__ void __launch_bounds__(ST, 6) k_powspec_rows(Pow2Args a) {
     const int lane = threadIdx.x & 31;
     double *sb = PRIV ? sbase + (threadIdx.x >> 5) * 4 * a.nbin : sbase;
     const int n2h = (int)a.n2h, az = (int)a.az;
-    // rows of contiguous cells: (x, y) rows along kz, or with zm (kz, x)
-    // rows along y (the layout torch's CUDA rfftn returns)
+    // rows of contiguous cells: (x, y) rows along kz for the (n0, n1, n2h)
+    // layout; with zm, (kz, x) rows along y of the (n2h, n0, n1) layout that
+    // torch's CUDA rfftn returns, which this kernel serves only for n1 < 32
+    // or n1 not a multiple of 32 (k_powspec_runs takes the others)
     // every index below fits in 32 bits (grids up to 2048: rows < 2^22,
     // bin-table indices < 2^31)
     const int n0 = (int)a.n0, n1 = (int)a.n1, h0 = a.h0, h1 = a.h1;
@@ -366,9 +368,9 @@ __global__ void __launch_bounds__(ST, 6) k_powspec_runs(Pow2Args a) {
     const int ax = (int)a.ax, ay = (int)a.ay, az = (int)a.az, nbin = a.nbin;
     const int R = n1 / 32, nrows = n2h * n0;
     const int wstride = gridDim.x * (ST / 32);
-    auto add = [&](int b, float pr, float pi, double kn, double nn) {
-        atomicAdd(sb + 4 * b + 1, (double)pr);
-        if (CROSS) atomicAdd(sb + 4 * b + 2, (double)pi);
+    auto add = [&](int b, double pr, double pi, double kn, double nn) {
+        atomicAdd(sb + 4 * b + 1, pr);
+        if (CROSS) atomicAdd(sb + 4 * b + 2, pi);
         if (GEOM) {
             atomicAdd(sb + 4 * b, kn);
             atomicAdd(sb + 4 * b + 3, nn);
@@ -384,8 +386,9 @@ __global__ void __launch_bounds__(ST, 6) k_powspec_runs(Pow2Args a) {
         const float2 *Fr = a.F + (int64_t)row * n1 + j0;
         const float2 *Gr = CROSS ? a.G + (int64_t)row * n1 + j0 : nullptr;
         int cur = nbin;
-        float ar = 0.f, ai = 0.f;
-        double ak = 0.0, an = 0.0;
+        // a run holds up to n1/32 cells: its sums are float64, so a long
+        // run rounds like the row kernel's per-32-cell float sums
+        double ar = 0.0, ai = 0.0, ak = 0.0, an = 0.0;
         for (int r = 0; r < R; ++r) {
             const int j = j0 + r;
             const int sj = j <= h1 / 2 ? j : j - h1;
@@ -394,8 +397,7 @@ __global__ void __launch_bounds__(ST, 6) k_powspec_runs(Pow2Args a) {
             if (b != cur) {
                 if (cur < nbin) add(cur, ar, ai, ak, an);
                 cur = b;
-                ar = ai = 0.f;
-                ak = an = 0.0;
+                ar = ai = ak = an = 0.0;
             }
             if (b < nbin) {
                 float pr = 0.f, pi = 0.f;
@@ -440,8 +442,8 @@ __global__ void __launch_bounds__(ST, 6) k_powspec_runs(Pow2Args a) {
                 const int src = __ffs(pending) - 1;
                 const int bb = __shfl_sync(0xffffffffu, b, src);
                 const bool mine = b == bb;
-                const float spr = warp_sumf(mine ? ar : 0.f);
-                const float spi = CROSS ? warp_sumf(mine ? ai : 0.f) : 0.f;
+                const double spr = warp_sum(mine ? ar : 0.0);
+                const double spi = CROSS ? warp_sum(mine ? ai : 0.0) : 0.0;
                 double sk = 0.0, sn = 0.0;
                 if (GEOM) {
                     sk = warp_sum(mine ? ak : 0.0);

@@ -51,6 +51,10 @@ def test_force_matches_oracle(cuda, ptcl, mesh, spacing):
 
 XPASS_CASES = [((32, 32, 32), 2, 1.0), ((32, 16, 24), 4, 2.0), ((64, 64, 64), 1, 2.0),
                ((128, 64, 32), 1, 1.0), ((128, 128, 128), 2, 2.0)]
+# x passes of 512 and 1024 points (the Split<512> and Split<1024> six-step
+# transforms the 512^3-particle / 1024^3-mesh run uses) on cheap anisotropic
+# meshes: (512, 32, 32), (1024, 32, 32), (1024, 64, 64)
+XPASS_LONG = [((128, 8, 8), 4, 1.0), ((256, 8, 8), 4, 1.0), ((256, 16, 16), 4, 1.0)]
 
 
 def _force_both_paths(cuda, gconf, pmid, disp, cot=None,
@@ -79,10 +83,11 @@ def _force_both_paths(cuda, gconf, pmid, disp, cot=None,
     return out
 
 
-@pytest.mark.parametrize('ptcl, mesh, spacing', XPASS_CASES)
+@pytest.mark.parametrize('ptcl, mesh, spacing', XPASS_CASES + XPASS_LONG)
 def test_fused_xpass_force_matches_oracle(cuda, ptcl, mesh, spacing):
-    """Power-of-two n0 (64..1024) takes the fused x-pass path (slab-wise
-    2-D cuFFT planes); it must match the oracle and the 3-D cuFFT path."""
+    """Power-of-two n0 (64..1024; the cases here reach 64, 128, 256, 512 and
+    1024) takes the fused x-pass path (slab-wise 2-D cuFFT planes); it must
+    match the oracle and the 3-D cuFFT path."""
     oconf, gconf, pmid, disp, vel = make(ptcl, mesh, spacing, 1.5 * spacing)
     acc_o = pm.gravity(pmid, disp, 0.3, oconf)
     fast, ref3d = _force_both_paths(cuda, gconf, pmid, disp)
@@ -91,7 +96,7 @@ def test_fused_xpass_force_matches_oracle(cuda, ptcl, mesh, spacing):
     assert rel_l2(fast, ref3d) < RTOL_ACC
 
 
-@pytest.mark.parametrize('ptcl, mesh, spacing', XPASS_CASES[:3])
+@pytest.mark.parametrize('ptcl, mesh, spacing', XPASS_CASES[:3] + XPASS_LONG)
 def test_fused_xpass_force_vjp_matches_oracle(cuda, ptcl, mesh, spacing):
     oconf, gconf, pmid, disp, vel = make(ptcl, mesh, spacing, 1.5 * spacing)
     cot = np.random.default_rng(12).normal(size=disp.shape).astype(np.float32)

@@ -74,12 +74,19 @@ def test_powspec_kernel_matches_oracle(cuda, shape, bins):
 
 
 @pytest.mark.parametrize('shape, bins', [((32, 64, 16), 1j / 3), ((64, 32, 32), 0.5),
-                                         ((2, 16, 32, 8), 2)])
+                                         ((2, 16, 32, 8), 2), ((32, 16, 32), 1j / 3),
+                                         ((16, 512, 16), 1j / 3), ((16, 512, 16), 1),
+                                         ((8, 1024, 8), 1j / 3), ((8, 1024, 8), 1)])
 def test_powspec_half_axis_major_layout(cuda, shape, bins):
     """torch's CUDA rfftn stores (n0, n1, n2h) half-axis major; the kernel
     bins that layout in place (pmx_powspec_bin_zmajor) and must give the
     sums of the transposed, contiguous copy (pmx_powspec_bin), also for a
-    cross spectrum and a leading batch axis."""
+    cross spectrum, a leading batch axis and the CIC deconvolution window.
+
+    n1 = 16 takes the row kernel's half-axis-major branch; n1 = 32..1024 the
+    run kernel, whose lanes walk runs of n1/32 cells: at n1 = 512 and 1024
+    a run of 16 or 32 cells crosses several bins (flushes inside a run) and
+    the lanes' last bins merge at the end of each row."""
     from pmwd_gb300 import spec_util as su
     rng = np.random.default_rng(7)
     f = torch.from_numpy(rng.normal(size=shape).astype(np.float32)).to(cuda)
@@ -87,15 +94,31 @@ def test_powspec_half_axis_major_layout(cuda, shape, bins):
     F, G = su.fftfwd(f, axes=(-3, -2, -1)), su.fftfwd(g, axes=(-3, -2, -1))
     grid = tuple(shape[-3:])
     bnum, bcut, edges, right = su._getbins(grid, bins, True)
-    for GG in (None, G):
+    for GG, deconv in ((None, None), (G, None), (None, 2)):
         su._GEOMETRY.clear()
-        k1, P1, N1 = su._bin_cuda(F, GG, grid, edges, right, bnum, None)
+        k1, P1, N1 = su._bin_cuda(F, GG, grid, edges, right, bnum, deconv)
         su._GEOMETRY.clear()
         k2, P2, N2 = su._bin_cuda(F.contiguous(), None if GG is None else GG.contiguous(), grid,
-                                  edges, right, bnum, None)
+                                  edges, right, bnum, deconv)
         np.testing.assert_allclose(k1.cpu().numpy(), k2.cpu().numpy(), rtol=1e-12)
         np.testing.assert_array_equal(N1.cpu().numpy(), N2.cpu().numpy())
         np.testing.assert_allclose(P1.cpu().numpy(), P2.cpu().numpy(), rtol=1e-5)
+
+
+@pytest.mark.parametrize('shape, bins', [((16, 512, 16), 1j / 3), ((8, 1024, 8), 1)])
+def test_powspec_long_runs_match_oracle(cuda, shape, bins):
+    """The run kernel at n1 = 512 and 1024 (runs of 16 and 32 cells per
+    lane) through the public powspec, against the oracle's float64
+    digitize/bincount, with and without the CIC deconvolution."""
+    from pmwd_gb300.spec_util import powspec
+    f = np.random.default_rng(8).normal(size=shape).astype(np.float32)
+    for deconv in (None, 2):
+        k_o, P_o, N_o, b_o = ics.powspec(f, 1.0, bins=bins, deconv=deconv)
+        k_g, P_g, N_g, b_g = powspec(torch.from_numpy(f).to(cuda), 1.0, bins=bins,
+                                     deconv=deconv)
+        np.testing.assert_array_equal(N_g.cpu().numpy(), N_o)
+        np.testing.assert_allclose(k_g.cpu().numpy(), k_o, rtol=1e-12)
+        np.testing.assert_allclose(P_g.cpu().numpy(), P_o, rtol=1e-5)
 
 
 @pytest.mark.parametrize('shape', [(2, 16, 18, 20), (2, 16, 32, 8)])
