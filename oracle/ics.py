@@ -7,9 +7,8 @@ spectrum (test infrastructure only).
 * ``lpt`` (2LPT)     pmwd/lpt.py:13-76, 136-212
 * ``powspec``        pmwd/spec_util.py:10-147
 
-White noise: the reference draws JAX threefry normals (modes.py:12-49);
-seeded NumPy PCG64 normals stand in, so realisations differ from the
-reference's but have the same distribution.
+* ``white_noise``    pmwd/modes.py:12-49, with JAX's Threefry normal draw
+  restated in ``oracle/prng.py`` (the reference's realisation of a seed)
 """
 
 import math
@@ -18,6 +17,7 @@ import numpy as np
 
 from . import cosmo as oc
 from . import pm
+from . import prng
 
 
 def gen_grid(conf):
@@ -42,9 +42,9 @@ def pos(pmid, disp, conf, wrap=True):
     return p
 
 
-def white_noise(seed, conf, real=False):
-    rng = np.random.default_rng(seed)
-    modes = rng.standard_normal(conf.ptcl_grid_shape, dtype=np.float32).astype(conf.float_dtype)
+def white_noise(seed, conf, real=False, layout='original'):
+    """modes.py:12-49 (Fourier or real modes; ``unit_abs`` not restated)."""
+    modes = prng.normal_f32(seed, conf.ptcl_grid_shape, layout).astype(conf.float_dtype)
     if real:
         return modes
     return pm.fftfwd(modes, norm='ortho')
@@ -114,9 +114,10 @@ def lpt(modes, cosmo, conf):
     return pmid, disp, vel
 
 
-def powspec(f, spacing, bins=1j / 3, cut_zero=True, cut_nyq=True):
+def powspec(f, spacing, bins=1j / 3, cut_zero=True, cut_nyq=True, deconv=None):
     """Spherically binned auto power spectrum, spec_util.py:10-147 (log bins
-    or linear bins; float64 accumulation)."""
+    or linear bins; float64 accumulation; ``deconv``: the sinc^-deconv
+    window of each axis, spec_util.py:115-116)."""
     f = np.asarray(f)
     grid_shape = f.shape[-3:]
     kfun = 1 / max(grid_shape)
@@ -138,6 +139,9 @@ def powspec(f, spacing, bins=1j / 3, cut_zero=True, cut_nyq=True):
     P = F.real.astype(np.float64) ** 2 + F.imag.astype(np.float64) ** 2
     kvec = pm.fftfreq(grid_shape, None, dtype=np.float64)
     k = np.sqrt(sum(kk ** 2 for kk in kvec))
+    if deconv is not None:
+        for kk in kvec:
+            P = P * np.sinc(kk) ** -deconv   # numpy's sinc has the pi
     k = np.broadcast_to(k, P.shape)
     N = np.full(P.shape, 2.0)
     N[..., 0] = 1
