@@ -120,6 +120,22 @@ typedef struct pmx_workspace pmx_workspace;
                               transforms with the cluster plane kernels
                               instead of slab-wise 2-D cuFFT (square
                               power-of-two planes 64..1024) */
+#define PMX_WS_VEC 16      /* deposit z-neighbour pairs that share an aligned
+                              group of four floats with one 16-byte vector
+                              reduction (n2 % 4 == 0; opt-in: slower on
+                              GB300) */
+#define PMX_WS_NO_GRAPH 32 /* issue the slab loops of the plane transforms
+                              directly instead of replaying captured graphs */
+#define PMX_WS_PLANE16 64  /* plane kernels in clusters of 16 CTAs (the
+                              non-portable size) instead of 8 */
+/* Slab-wise plane transforms: number of concurrent chains (1..4; 0 = the
+ * default 2) and log2 of the x-planes per cuFFT execution (1..15; 0 = the
+ * default, the smallest power of two >= 8 reaching 32 MB), packed into the
+ * flags.  Results do not depend on either. */
+#define PMX_WS_CHAINS_SHIFT 8
+#define PMX_WS_SLAB_SHIFT 12
+#define PMX_WS_CHAINS(k) (((k) & 7) << PMX_WS_CHAINS_SHIFT)
+#define PMX_WS_SLAB_LOG2(s) (((s) & 15) << PMX_WS_SLAB_SHIFT)
 
 /* Device bytes a workspace for this 3-D mesh allocates (meshes, spectra,
  * cuFFT work areas, reduction scratch). */
@@ -293,6 +309,29 @@ int pmx_powspec_bin_zmajor(const float *F, const float *G, int64_t nbatch,
                            const double *ky, const double *kz, const double *edges,
                            int32_t nedges, int32_t right, int32_t nbin, double deconv,
                            double *ksum, double *psum, double *nsum, void *stream);
+
+/* --------------------------------------------------------------------------
+ * White noise (pmwd/modes.py:12-49 ``white_noise``)
+ * ------------------------------------------------------------------------ */
+
+/* Counter layouts of JAX's Threefry-2x32 bits: ORIGINAL is JAX's
+ * jax_threefry_partitionable=False (its default before JAX 0.5, the one
+ * pmwd's published outputs were drawn with); PARTITIONABLE is JAX's default
+ * since 0.5. */
+#define PMX_PRNG_ORIGINAL       0
+#define PMX_PRNG_PARTITIONABLE  1
+
+/* out[0..n) = jax.random.bits(key, (n,), uint32) for the Threefry key
+ * (k0, k1) -- jax.random.PRNGKey(seed) is (seed >> 32, seed & 0xffffffff).
+ * The original layout covers n <= 2^32 - 2. */
+int pmx_random_bits(uint32_t k0, uint32_t k1, int64_t n, int layout, uint32_t *out,
+                    void *stream);
+
+/* out[0..n) = jax.random.normal(key, (n,), float32), the draw of
+ * modes.py:33-36: sqrt(2) erfinv(u) of a uniform u in [nextafter(-1, 0), 1)
+ * built from the bits above, erfinv by Giles' single-precision
+ * approximation. */
+int pmx_normal(uint32_t k0, uint32_t k1, int64_t n, int layout, float *out, void *stream);
 
 /* --------------------------------------------------------------------------
  * Growth functions (host)

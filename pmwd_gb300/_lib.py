@@ -70,6 +70,8 @@ SIGNATURES = {
     'pmx_powspec_bin_zmajor': (c_int, [c_p, c_p, c_i64, ctypes.POINTER(c_i64), c_p, c_p, c_p, c_p,
                                        c_i32, c_i32, c_i32, c_d, c_p, c_p, c_p, c_p]),
     'pmx_growth_ode': (c_int, [c_p, c_i64, c_p, c_i64, c_d, c_d, c_p, c_p]),
+    'pmx_random_bits': (c_int, [ctypes.c_uint32, ctypes.c_uint32, c_i64, c_int, c_p, c_p]),
+    'pmx_normal': (c_int, [ctypes.c_uint32, ctypes.c_uint32, c_i64, c_int, c_p, c_p]),
     'pmx_profile_enable': (c_int, [c_p, c_int]),
     'pmx_profile_read': (c_int, [c_p, ctypes.POINTER(c_d), ctypes.POINTER(c_i64),
                                  ctypes.POINTER(c_i64)]),
@@ -95,6 +97,11 @@ PMX_WS_ADJOINT = 1
 PMX_WS_CUFFT3D = 2
 PMX_WS_WINDOW = 4
 PMX_WS_PLANE = 8
+PMX_WS_VEC = 16
+PMX_WS_NO_GRAPH = 32
+PMX_WS_PLANE16 = 64
+PMX_WS_CHAINS_SHIFT = 8
+PMX_WS_SLAB_SHIFT = 12
 
 _lib = None
 _lock = threading.Lock()
@@ -171,12 +178,22 @@ class Workspace:
     """Owner of a ``pmx_workspace`` (mesh buffers, spectra, cuFFT plans)."""
 
     def __init__(self, mesh_shape, adjoint=True, device=None, cufft3d=False, window=False,
-                 plane=False):
+                 plane=False, vec=False, graphs=True, plane16=False, chains=0, slab_log2=0):
+        """Flags of pmx_workspace_create (include/pmx.h): ``cufft3d`` 3-D
+        cuFFT plans instead of the fused x pass, ``window`` warp-window
+        deposits, ``plane`` cluster plane kernels (``plane16``: clusters of
+        16), ``vec`` vector z-pair reductions, ``graphs`` slab loops as CUDA
+        graphs, ``chains`` concurrent slab chains and ``slab_log2`` planes
+        per cuFFT execution (0: defaults)."""
         load()
         self.mesh_shape = tuple(int(s) for s in mesh_shape)
         self.adjoint = adjoint
         flags = ((PMX_WS_ADJOINT if adjoint else 0) | (PMX_WS_CUFFT3D if cufft3d else 0)
-                 | (PMX_WS_WINDOW if window else 0) | (PMX_WS_PLANE if plane else 0))
+                 | (PMX_WS_WINDOW if window else 0) | (PMX_WS_PLANE if plane else 0)
+                 | (PMX_WS_VEC if vec else 0) | (0 if graphs else PMX_WS_NO_GRAPH)
+                 | (PMX_WS_PLANE16 if plane16 else 0)
+                 | ((int(chains) & 7) << PMX_WS_CHAINS_SHIFT)
+                 | ((int(slab_log2) & 15) << PMX_WS_SLAB_SHIFT))
         self.device = torch.device('cuda', torch.cuda.current_device() if device is None else device)
         shp = (c_i64 * 3)(*self.mesh_shape)
         h = c_p()

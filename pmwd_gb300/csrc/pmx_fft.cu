@@ -974,17 +974,10 @@ bool plane_supported(int64_t n1, int64_t n2) {
     return n1 == n2 && (n1 == 64 || n1 == 128 || n1 == 256 || n1 == 512 || n1 == 1024);
 }
 
-// Cluster size of the plane kernels: PMX_PLANE_CLUSTER (8 or 16), else 8.
-int plane_cluster() {
-    const char *e = std::getenv("PMX_PLANE_CLUSTER");
-    return e && std::atoi(e) == 16 ? 16 : 8;
-}
-
-int plane_max_clusters(int64_t n1, int64_t n2, int *ncl) {
+int plane_max_clusters(int64_t n1, int64_t n2, bool c16, int *ncl) {
     if (!plane_supported(n1, n2)) return fail(PMX_ERR_SHAPE, "plane transform needs square power-of-two planes 64..1024");
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
-    const bool c16 = plane_cluster() == 16;
     int a = 0, b = 0;
     cudaError_t e = cudaSuccess;
 #define PMX_PLANE_Q(N1_, L_)                                                                       \
@@ -1010,10 +1003,9 @@ int plane_max_clusters(int64_t n1, int64_t n2, int *ncl) {
 }
 
 int plane_fft(bool inv, const void *in, void *out, const float2 *ptw, int64_t nplanes, int64_t n1,
-              int64_t n2, float2 *scratch, int max_clusters, cudaStream_t st) {
+              int64_t n2, float2 *scratch, int max_clusters, bool c16, cudaStream_t st) {
     if (!plane_supported(n1, n2)) return fail(PMX_ERR_SHAPE, "plane transform needs square power-of-two planes 64..1024");
     if (nplanes < 1) return PMX_OK;
-    const bool c16 = plane_cluster() == 16;
 #define PMX_PLANE_L(N1_, L_)                                                                       \
     return c16 ? launch_plane<N1_, L_, 16>(inv, in, out, ptw, nplanes, scratch, max_clusters, st)  \
                : launch_plane<N1_, L_, 8>(inv, in, out, ptw, nplanes, scratch, max_clusters, st);

@@ -102,6 +102,8 @@ struct pmx_workspace {
     // square power-of-two planes: the (y, z) transforms are the cluster
     // plane kernels of pmx_fft.cu instead of 2-D cuFFT
     bool plane = false;
+    bool plane16 = false;       // clusters of 16 CTAs instead of 8
+    bool vec = false;           // vector z-pair reductions (n2 % 4 == 0)
     float2 *ptw = nullptr;      // plane_twiddles(n1, n2)
     float2 *pscr = nullptr;     // c2r scratch: one n1 x n2p plane per cluster
     int pcl = 0;                // clusters the scratch serves
@@ -1011,9 +1013,8 @@ int check_hot(pmx_workspace *ws, const pmx_enmesh_spec *spec, const void *pmid, 
     h->vcomp = nullptr;
     h->win = ws->win;
     // measured slower on GB300 (the v4 reductions with two zero lanes cost
-    // more than the scalar atomics they replace): opt-in with PMX_VEC=1
-    const char *venv = std::getenv("PMX_VEC");
-    h->vec = ws->n2 % 4 == 0 && venv && venv[0] == '1';
+    // more than the scalar atomics they replace): opt-in, PMX_WS_VEC
+    h->vec = ws->vec;
     if (ws->xfast) {
         h->gxs = 2 * ws->n1 * ws->n2;
         h->gjs = ws->n1 * ws->n2;
@@ -1115,7 +1116,7 @@ int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t s
         if (ws->plane) {
             Stage sg(ws, 2, st, 1);
             int st2 = plane_fft(false, ws->dens, H, ws->ptw, ws->n0, ws->n1, ws->n2, ws->pscr,
-                                ws->pcl, st);
+                                ws->pcl, ws->plane16, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 2, st, 0);
@@ -1131,7 +1132,7 @@ int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t s
         if (ws->plane) {
             Stage sg(ws, 4, st, 1);
             int st2 = plane_fft(true, ws->ck, ws->g, ws->ptw, 3 * ws->n0, ws->n1, ws->n2, ws->pscr,
-                                ws->pcl, st);
+                                ws->pcl, ws->plane16, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 4, st, 0);
@@ -1170,7 +1171,7 @@ int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
         if (ws->plane) {
             Stage sg(ws, 8, st, 1);
             int st2 = plane_fft(false, ws->mcot, ws->ck, ws->ptw, 3 * ws->n0, ws->n1, ws->n2,
-                                ws->pscr, ws->pcl, st);
+                                ws->pscr, ws->pcl, ws->plane16, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 8, st, 0);
@@ -1186,7 +1187,7 @@ int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
         if (ws->plane) {
             Stage sg(ws, 10, st, 1);
             int st2 = plane_fft(true, Sk, ws->rcot, ws->ptw, ws->n0, ws->n1, ws->n2, ws->pscr,
-                                ws->pcl, st);
+                                ws->pcl, ws->plane16, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 10, st, 0);
@@ -1241,17 +1242,13 @@ int make_plan2d(cufftHandle *plan, int64_t n1, int64_t n2, cufftType type, int64
     return PMX_OK;
 }
 
-// x-planes per 2-D cuFFT execution: PMX_SLAB if set, else 8, so that the
-// intermediate of every concurrent execution stays in L2 (the slab loops run
-// as captured CUDA graphs, which removes the per-call launch cost).
 // x-planes per slab execution of the (y, z) plane transforms: the smallest
 // power of two >= 8 whose complex planes reach 32 MB (8 planes at 1024^2,
 // every plane of meshes up to 128^3), so small meshes take a few large
-// cuFFT launches instead of many tiny ones.  PMX_SLAB overrides.
-int64_t choose_slab(int64_t n0, int64_t n1, int64_t n2) {
-    const char *env = std::getenv("PMX_SLAB");
-    int64_t S = 0;
-    if (env) S = std::atoll(env);
+// cuFFT launches instead of many tiny ones.  A nonzero log2 (the
+// PMX_WS_SLAB_LOG2 field of the flags) sets it instead.
+int64_t choose_slab(int64_t n0, int64_t n1, int64_t n2, int log2) {
+    int64_t S = log2 > 0 ? (int64_t)1 << log2 : 0;
     if (S <= 0) {
         const int64_t plane = n1 * (n2 / 2 + 1) * 8;
         S = 8;
@@ -1360,11 +1357,10 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
         }
         return PMX_OK;
     };
-    const char *xenv = std::getenv("PMX_XFAST");
-    ws->xfast = xpass_supported(ws->n0) && !(flags & PMX_WS_CUFFT3D) && !(xenv && xenv[0] == '0');
-    const char *penv = std::getenv("PMX_PLANE");
-    ws->plane = ws->xfast && plane_supported(ws->n1, ws->n2) &&
-                ((flags & PMX_WS_PLANE) || (penv && penv[0] == '1')) && !(penv && penv[0] == '0');
+    ws->xfast = xpass_supported(ws->n0) && !(flags & PMX_WS_CUFFT3D);
+    ws->plane = ws->xfast && plane_supported(ws->n1, ws->n2) && (flags & PMX_WS_PLANE);
+    ws->plane16 = (flags & PMX_WS_PLANE16) != 0;
+    ws->vec = ws->n2 % 4 == 0 && (flags & PMX_WS_VEC);
     ws->n2p = ws->plane ? padded_row(ws->n2h) : ws->n2h;
     int64_t ktn = 2 * (ws->n0 + ws->n1 + ws->n2h);
     if ((st = alloc((void **)&ws->dens, ws->M * 4)) ||
@@ -1377,9 +1373,7 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
     }
     // rcot behind the complex spectrum held in g (2 n0 n1 n2p + M <= 3 M floats)
     ws->rcot = ws->g + 2 * ws->n0 * ws->n1 * ws->n2p;
-    const char *wenv = std::getenv("PMX_WIN");
-    ws->win = (ws->n2 % 4 == 0) && ((flags & PMX_WS_WINDOW) || (wenv && wenv[0] == '1')) &&
-              !(wenv && wenv[0] == '0');
+    ws->win = (ws->n2 % 4 == 0) && (flags & PMX_WS_WINDOW);
     if (ws->win) {
         cudaError_t e = cudaFuncSetAttribute(k_g3adj<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)WIN3_SMEM);
@@ -1392,7 +1386,7 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
     cufftHandle *ph[4];
     bool *hv[4];
     if (ws->plane) {
-        if ((st = plane_max_clusters(ws->n1, ws->n2, &ws->pcl)) ||
+        if ((st = plane_max_clusters(ws->n1, ws->n2, ws->plane16, &ws->pcl)) ||
             (st = alloc((void **)&ws->pscr, (size_t)ws->pcl * ws->n1 * ws->n2p * sizeof(float2)))) {
             ws_free(ws);
             return st;
@@ -1408,14 +1402,13 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
         }
     }
     if (ws->xfast) {
-        ws->slab = choose_slab(ws->n0, ws->n1, ws->n2);
+        ws->slab = choose_slab(ws->n0, ws->n1, ws->n2, (flags >> PMX_WS_SLAB_SHIFT) & 15);
         const int64_t S = ws->slab;
         if (!ws->plane) {
-            const char *kenv = std::getenv("PMX_SLAB_CHAINS");
-            const char *genv = std::getenv("PMX_SLAB_GRAPH");
-            int K = kenv ? std::atoi(kenv) : 2;
-            ws->nbranch = K < 1 ? 1 : (K > KMAX ? KMAX : K);
-            ws->graphs = !(genv && genv[0] == '0');
+            const int kf = (flags >> PMX_WS_CHAINS_SHIFT) & 7;
+            const int K = kf ? kf : 2;   // two concurrent chains measured best
+            ws->nbranch = K > KMAX ? KMAX : K;
+            ws->graphs = !(flags & PMX_WS_NO_GRAPH);
             auto mk_stream = [&](cudaStream_t *sp) -> int {
                 cudaError_t e = cudaStreamCreateWithFlags(sp, cudaStreamNonBlocking);
                 return e == cudaSuccess ? PMX_OK : cuda_status(e, "cudaStreamCreate");

@@ -92,9 +92,10 @@ void xpass_twiddles(int64_t n, float2 *host);
 // complex values each, plane_max_clusters of them).  One thread-block cluster
 // per plane.  ptw holds plane_twiddles(n1, n2) (2 n1 + 1 entries).
 bool plane_supported(int64_t n1, int64_t n2);
-int plane_max_clusters(int64_t n1, int64_t n2, int *ncl);
+// c16: clusters of 16 CTAs (non-portable size) instead of 8.
+int plane_max_clusters(int64_t n1, int64_t n2, bool c16, int *ncl);
 int plane_fft(bool inv, const void *in, void *out, const float2 *ptw, int64_t nplanes, int64_t n1,
-              int64_t n2, float2 *scratch, int max_clusters, cudaStream_t st);
+              int64_t n2, float2 *scratch, int max_clusters, bool c16, cudaStream_t st);
 void plane_twiddles(int64_t n1, int64_t n2, float2 *host);
 
 __device__ __forceinline__ int pymod(int x, int m) {

@@ -1,9 +1,12 @@
 """White noise and linear modes (pmwd/modes.py:1-117), torch on the GPU.
 
-White noise is drawn from NumPy's PCG64 generator on the host (float32
-standard normals, then uploaded), so a seed gives the same field on every
-machine; the reference draws JAX threefry normals instead, so realisations
-differ from the reference's while the distribution is the same.
+White noise is drawn on the GPU by libpmx's ``pmx_normal``, which restates
+the draw of the reference, ``jax.random.normal(jax.random.PRNGKey(seed),
+shape, float32)`` (modes.py:33-36): Threefry-2x32 bits in JAX's counter
+layout, a uniform in [nextafter(-1, 0), 1) and sqrt(2) erfinv(u).  A seed
+therefore gives pmwd's own realisation.  JAX changed its default counter
+layout in version 0.5 (``jax_threefry_partitionable``); the default here,
+``'original'``, is the layout of pmwd's published outputs.
 """
 
 import math
@@ -18,11 +21,29 @@ from .boltzmann import linear_power
 from .pm_util import fftfreq, fftfwd, fftinv
 
 
-def white_noise(seed, conf, real=False, unit_abs=False, device=None):
-    """White noise Fourier or real modes (modes.py:12-49)."""
+PRNG_LAYOUTS = {'original': 0, 'partitionable': 1}
+
+
+def prng_key(seed):
+    """jax.random.PRNGKey of an int64 seed (64-bit JAX types, as pmwd turns
+    on): the uint32 pair (seed >> 32, seed & 0xffffffff)."""
+    s = int(np.int64(seed)) & 0xFFFFFFFFFFFFFFFF
+    return s >> 32, s & 0xFFFFFFFF
+
+
+def white_noise(seed, conf, real=False, unit_abs=False, device=None, prng_layout='original'):
+    """White noise Fourier or real modes (modes.py:12-49), the reference's
+    own draw for the same seed (``prng_layout``: JAX's Threefry counter
+    layout, 'original' before JAX 0.5 or 'partitionable' after)."""
+    from . import _lib
     dev = device if device is not None else torch.device('cuda', torch.cuda.current_device())
-    rng = np.random.default_rng(seed)
-    modes = torch.from_numpy(rng.standard_normal(conf.ptcl_grid_shape, dtype=np.float32)).to(dev)
+    if prng_layout not in PRNG_LAYOUTS:
+        raise ValueError(f'{prng_layout=} not in {tuple(PRNG_LAYOUTS)}')
+    k0, k1 = prng_key(seed)
+    modes = torch.empty(conf.ptcl_grid_shape, dtype=torch.float32, device=dev)
+    with torch.cuda.device(dev):
+        _lib.call('pmx_normal', k0, k1, modes.numel(), PRNG_LAYOUTS[prng_layout], modes,
+                  _lib.stream_ptr(dev))
     if real and not unit_abs:
         return modes
     modes = fftfwd(modes, norm='ortho')
