@@ -55,6 +55,12 @@ def parse():
                     help='particle grid side of the bounded CPU sample')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-full-run', action='store_true',
+                    help='skip the whole-run measurement (all forward steps, then all adjoint '
+                         'steps)')
+    ap.add_argument('--dry-run', action='store_true',
+                    help='no GPU work: each rank reports a fixed synthetic time, to check the '
+                         'replica launch and the reduction over ranks on CPU (gloo)')
     ap.add_argument('--serve', type=int, default=0,
                     help='serving mode: number of requests of the serving stream')
     ap.add_argument('--serve-sides', default='64,128,256')
@@ -320,6 +326,7 @@ def run_pmx(args, rank, world, local_rank):
     pmid = ptcl.pmid.contiguous()
     disp = ptcl.disp.contiguous()
     vel = ptcl.vel.contiguous()
+    disp0, vel0 = disp.clone(), vel.clone()   # the initial state of the whole-run measurement
     acc = torch.empty_like(disp)
     g = torch.Generator(device=dev)
     g.manual_seed(1234 + rank)
@@ -452,6 +459,12 @@ def run_pmx(args, rank, world, local_rank):
                                     'buffers copied in and out every step (one copy stream '
                                     'per buffer)'}
 
+    # ---- the whole run: every forward step, then every adjoint step ----
+    full = None
+    if not args.no_full_run:
+        full = full_run(lib, ws, spec, pmid, disp0, vel0, disp_cot, vel_cot, alpha, acc, N,
+                        fwd32, adj32, Om, stream, dev, world, local_rank, barrier)
+
     if rank != 0:
         return
 
@@ -507,9 +520,88 @@ def run_pmx(args, rank, world, local_rank):
         'forward_only': {'ms_per_step': ms_fwd, 'value': N / (ms_fwd / 1e3), 'unit': UNIT,
                          'note': 'forward half of the timed segment (the metric of the '
                                  'reference\'s published per-step N-body timings)'},
+        'full_run': None if full is None else dict(
+            full, step_roofline_frac=step_bytes / (full['ms_per_step'] / 1e3) / 1e9 / peak),
         'clocks': clk,
     }
     print(json.dumps(line), flush=True)
+
+
+def full_run(lib, ws, spec, pmid, disp0, vel0, disp_cot, vel_cot, alpha, acc, N, fwd32, adj32,
+             Om, stream, dev, world, local_rank, barrier):
+    """All steps of the run from the 2LPT state, as nbody() and its backward
+    execute them: force at a_start, every forward step in one multi-step
+    call, the force VJP at a_stop, every adjoint step in one multi-step call
+    (late, clustered steps included, where the timed segment has the first
+    steps only).  Rates per fwd+adj step pair."""
+    import torch
+    from pmwd_gb300 import _lib
+    P = _lib.ptr
+    nsteps = fwd32.shape[0]
+    disp, vel = disp0.clone(), vel0.clone()
+    dd = torch.zeros((nsteps + 1, 4), dtype=torch.float64, device=dev)
+    sp = _lib.c_p(stream.cuda_stream)
+    e0, em, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    lib.pmx_profile_enable(ws.handle, 1)
+    barrier()
+    e0.record(stream)
+    _lib.check(lib.pmx_force(ws.handle, spec, P(pmid), P(disp), N, N, Om, P(acc), sp), 'force')
+    _lib.check(lib.pmx_nbody_steps(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc), N, N, nsteps,
+                                   fwd32.ctypes.data_as(ctypes.c_void_p), Om, sp),
+               'pmx_nbody_steps')
+    em.record(stream)
+    _lib.check(lib.pmx_force_vjp(ws.handle, spec, P(pmid), P(disp), N, N, Om, P(vel_cot), P(acc),
+                                 P(alpha), P(dd[nsteps, 3:]), sp), 'pmx_force_vjp')
+    _lib.check(lib.pmx_nbody_adj_steps(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc),
+                                       P(disp_cot), P(vel_cot), P(alpha), N, N, nsteps,
+                                       adj32.ctypes.data_as(ctypes.c_void_p), Om, P(dd), sp),
+               'pmx_nbody_adj_steps')
+    e1.record(stream)
+    barrier()
+    lib.pmx_profile_enable(ws.handle, 0)
+    clk = clocks.stop()
+    stages, launches = _lib.profile_read(ws)
+    ms, value = replica_throughput(e0.elapsed_time(e1), N * nsteps, world, dev)
+    back = float((disp - disp0).norm() / disp0.norm())
+    return {'steps': nsteps, 'ms_total': ms, 'ms_per_step': ms / nsteps, 'value': value,
+            'unit': UNIT, 'forward_ms_per_step': e0.elapsed_time(em) / nsteps,
+            'adjoint_ms_per_step': em.elapsed_time(e1) / nsteps,
+            'stages_ms_per_step': {k: v[0] / nsteps for k, v in stages.items() if v[1]},
+            'gpu_launches': launches, 'reversibility_rel_disp': back, 'clocks': clk}
+
+
+def run_dry(args, rank, world):
+    """The replica launch without GPU work: each rank reports (100 + 10 rank)
+    ms for N K particle-steps; rank 0 prints the reduced line."""
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group('gloo')
+    n = args.ptcl ** 3
+    ms, value = replica_throughput(100.0 + 10.0 * rank, n * args.steps, world, 'cpu')
+    if rank == 0:
+        print(json.dumps({'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
+                          'steps': args.steps, 'ms_per_step': ms / args.steps, 'dry_run': True,
+                          'config': workload_config(args, world)}), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def launch_replicas(args):
+    """``--gpus N`` outside torchrun: start N ranks (one replica simulation
+    per GPU) with torch.distributed.run on this node and pass their output
+    through; the exit status is the launcher's."""
+    import socket
+    s = socket.socket()
+    s.bind(('127.0.0.1', 0))
+    port = s.getsockname()[1]
+    s.close()
+    cmd = [sys.executable, '-m', 'torch.distributed.run', '--nnodes=1',
+           f'--nproc-per-node={args.gpus}', '--master-addr', '127.0.0.1', '--master-port',
+           str(port), os.path.abspath(__file__), *sys.argv[1:]]
+    return subprocess.call(cmd)
 
 
 def run_serve(args):
@@ -805,11 +897,16 @@ def run_powspec(args):
 
 def main():
     args = parse()
+    if args.gpus > 1 and 'WORLD_SIZE' not in os.environ and args.impl == 'pmx':
+        sys.exit(launch_replicas(args))
     rank = int(os.environ.get('RANK', 0))
     world = int(os.environ.get('WORLD_SIZE', 1))
     local_rank = int(os.environ.get('LOCAL_RANK', 0))
     if args.impl == 'reference':
         run_reference(args, rank)
+        return
+    if args.dry_run:
+        run_dry(args, rank, world)
         return
     if args.serve:
         if rank == 0:

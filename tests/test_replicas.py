@@ -50,3 +50,24 @@ def test_replica_throughput_single_rank():
     import bench
     ms, value = bench.replica_throughput(50.0, 500, 1, 'cpu')
     assert ms == 50.0 and value == pytest.approx(10000.0)
+
+
+def test_bench_gpus_flag_launches_replicas():
+    """``bench.py --gpus 2`` outside torchrun starts two ranks itself (one
+    replica per GPU); with --dry-run they do no GPU work and report
+    100 + 10 rank ms, so the printed line must carry n_gpus 2, the slowest
+    rank's time and both ranks' particle-steps."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, 'bench.py'), '--gpus', '2', '--dry-run',
+                        '--steps', '3', '--ptcl', '8'], cwd=root, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith('{')]
+    assert len(lines) == 1, r.stdout
+    line = json.loads(lines[0])
+    assert line['n_gpus'] == 2 and line['dry_run']
+    assert line['ms_per_step'] == pytest.approx(110.0 / 3)
+    assert line['value'] == pytest.approx(2 * 8 ** 3 * 3 / 0.110)
