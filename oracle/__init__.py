@@ -14,7 +14,11 @@ this oracle was written, so it could not be run to produce golden vectors.
 The oracle is pinned by (i) the known-answer properties of the reference's
 own test file ``tests/pm_test.py`` (centred-particle scatter, scatter sum,
 uniform gather, reversibility), (ii) adjoint checks against autograd of an
-independent float64 torch restatement (``oracle.ad``), and (iii) published
-statistics printed in ``docs/examples/quickstart.ipynb``.  Element-wise
-end-to-end values of the reference itself are therefore "parity unpinned".
+independent float64 torch restatement (``oracle.ad``), (iii) the
+white-noise draw restated from JAX's published algorithm (``oracle.prng``,
+checked against the Random123 known answers and JAX's documented draws), so
+that a seed gives pmwd's own realisation, and (iv) through it, outputs pmwd
+published for seeded runs (``tests/golden/published_pmwd.json``: the
+quickstart notebook's statistics and cosmology gradients, the adjoint
+paper's 64 repeated gradient runs), which the GPU path reproduces.
 """

@@ -261,10 +261,16 @@ def test_multistep_equals_single_steps(cuda, nb_case):
     for a, b in zip(out[0][0], out[2][0]):
         assert rel_l2(b, a) < 1e-5
     names = ('disp', 'vel', 'acc', 'disp_cot', 'vel_cot', 'dots')
+    cot_full = 0.0
     for name, a, a2, b in zip(names, out[0][1], out[1][1], out[2][1]):
         floor = rel_l2(a2, a)
         full = rel_l2(b, a)
-        if name.endswith('_cot'):
+        if name == 'dots':
+            # the dots are sums over the cotangents: a particle whose
+            # cotangent jumped at a cell boundary (below) moves them too
+            assert full < max(1e-3, 10 * floor, 2 * cot_full), (name, full, floor, cot_full)
+        elif name.endswith('_cot'):
+            cot_full = max(cot_full, full)
             # The CIC weight gradient is piecewise constant: a rounding-level
             # difference in a reconstructed position can move a particle
             # across a cell boundary and change its cotangent by O(1) (about
