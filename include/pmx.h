@@ -37,14 +37,19 @@ extern "C" {
  * call it: grid 1 is the particle grid of conf (cell size a1 =
  * conf.cell_size, periodic shape s1 = conf.mesh_shape); grid 2 is the target
  * mesh with spatial shape mesh_shape, origin offset b12 and cell size a2
- * (cell_size <= 0 means the reference's ``cell_size=None``). */
+ * (cell_size <= 0 means the reference's ``cell_size=None``).  All
+ * wrap_shape entries 0 means s1 = None (no periodic wrapping,
+ * particles.py:212-254 with wrap=False); then `drop` != 0 replaces negative
+ * indices by mesh_shape, as the reference does with s2 given. */
 typedef struct pmx_enmesh_spec {
     int32_t dim;             /* spatial dimension, 1..3                    */
-    int32_t wrap_shape[3];   /* conf.mesh_shape (s1), first `dim` used     */
+    int32_t wrap_shape[3];   /* conf.mesh_shape (s1), first `dim` used;
+                                all 0: no wrapping                         */
     int64_t mesh_shape[3];   /* spatial shape of the mesh array (s2)       */
     double  conf_cell_size;  /* conf.cell_size (a1)                        */
     double  offset[3];       /* offset of mesh to particle grid (b12)      */
     double  cell_size;       /* mesh cell size a2, <= 0 for None           */
+    int32_t drop;            /* without wrapping: negative indices -> s2   */
 } pmx_enmesh_spec;
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -63,8 +68,9 @@ int pmx_device_sms(int *sms);
 /* Multilinear indices, fractions and fraction gradients of every particle,
  * pmwd/particles.py:212-254 ``ptcl_enmesh`` -> pm_util.py:33-156.
  * ind (n, 2^dim, dim) int32, frac (n, 2^dim), frac_grad (n, 2^dim, dim);
- * ind and frac_grad may be NULL.  Indices are bit-exact with the reference
- * (wrapped by s1, never dropped). */
+ * ind and frac_grad may be NULL.  Indices are bit-exact with the reference's
+ * int16 indices: wrapped by s1, or without wrapping the int16 sums, negative
+ * ones replaced by s2 when spec->drop is set. */
 int pmx_enmesh(const pmx_enmesh_spec *spec, const int16_t *pmid,
                const float *disp, int64_t n, int32_t *ind, float *frac,
                float *frac_grad, void *stream);
@@ -275,6 +281,53 @@ int pmx_nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec,
                         float *acc_cot, int64_t n, int64_t ptcl_num,
                         int32_t nsteps, const float *factors, double omega_m,
                         double *dots, void *stream);
+
+/* --------------------------------------------------------------------------
+ * Batched simulations: several independent runs that share a mesh shape and
+ * cell size advance in one call (pmwd runs one simulation per call,
+ * nbody.py:215-276; this is the serving form).  Each simulation occupies one
+ * slot of a batched workspace: every particle kernel launch serves all of
+ * them (one block row per simulation), and each plane transform runs over
+ * all their planes at once.  A simulation's arithmetic is the one of the
+ * single-simulation entry points, so its result is the same alone and in a
+ * batch up to the order of float32 atomic adds.
+ * ------------------------------------------------------------------------ */
+
+/* One simulation of a batched call.  Particle and cotangent arrays are
+ * DEVICE memory (n, 3); factors is HOST memory, (nsteps, 3) as for
+ * pmx_nbody_steps / pmx_nbody_adj_steps; dots is DEVICE memory, (nsteps + 1,
+ * 4), used by the adjoint call only. */
+typedef struct pmx_sim {
+    const int16_t *pmid;
+    float *disp, *vel, *acc;
+    float *disp_cot, *vel_cot, *acc_cot;
+    int64_t n, ptcl_num;
+    double omega_m;
+    const float *factors;
+    double *dots;
+} pmx_sim;
+
+/* A workspace whose buffers hold `slots` simulations (1..16) of the same
+ * mesh shape; pmx_workspace_create is the case slots = 1.  Batched calls
+ * need the fused x-pass path (n0 a power of two in 64..1024) and the plain
+ * deposits (no PMX_WS_WINDOW). */
+int pmx_workspace_create_batch(const int64_t mesh_shape[3], int32_t flags,
+                               int32_t slots, pmx_workspace **ws);
+int pmx_workspace_slots(const pmx_workspace *ws, int32_t *slots);
+
+/* For each of the nsim simulations (nsim <= slots): with init_force, first
+ * acc = F(disp) as pmx_force; then nsteps steps as pmx_nbody_steps. */
+int pmx_nbody_steps_batch(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                          int32_t nsim, const pmx_sim *sims, int32_t init_force,
+                          int32_t nsteps, void *stream);
+
+/* For each of the nsim simulations: with init_vjp, first the force VJP at
+ * the current positions with acc_cot = vel_cot, as pmx_force_vjp (acc,
+ * acc_cot written; the Omega_m term into dots[4 nsteps + 3]); then nsteps
+ * reverse steps as pmx_nbody_adj_steps (dots rows 0..nsteps-1). */
+int pmx_nbody_adj_steps_batch(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                              int32_t nsim, const pmx_sim *sims, int32_t init_vjp,
+                              int32_t nsteps, void *stream);
 
 /* --------------------------------------------------------------------------
  * Power spectrum (pmwd/spec_util.py:50-147)

@@ -24,7 +24,15 @@ c_int = ctypes.c_int
 class EnmeshSpec(ctypes.Structure):
     """``pmx_enmesh_spec`` (include/pmx.h)."""
     _fields_ = [('dim', c_i32), ('wrap_shape', c_i32 * 3), ('mesh_shape', c_i64 * 3),
-                ('conf_cell_size', c_d), ('offset', c_d * 3), ('cell_size', c_d)]
+                ('conf_cell_size', c_d), ('offset', c_d * 3), ('cell_size', c_d),
+                ('drop', c_i32)]
+
+
+class PmxSim(ctypes.Structure):
+    """``pmx_sim`` (include/pmx.h): one simulation of a batched call."""
+    _fields_ = [('pmid', c_p), ('disp', c_p), ('vel', c_p), ('acc', c_p), ('disp_cot', c_p),
+                ('vel_cot', c_p), ('acc_cot', c_p), ('n', c_i64), ('ptcl_num', c_i64),
+                ('omega_m', c_d), ('factors', c_p), ('dots', c_p)]
 
 
 # name -> (restype, argtypes); every entry point of include/pmx.h
@@ -43,6 +51,13 @@ SIGNATURES = {
     'pmx_workspace_bytes': (c_int, [ctypes.POINTER(c_i64), c_i32, ctypes.POINTER(ctypes.c_size_t)]),
     'pmx_workspace_create': (c_int, [ctypes.POINTER(c_i64), c_i32, ctypes.POINTER(c_p)]),
     'pmx_workspace_destroy': (c_int, [c_p]),
+    'pmx_workspace_create_batch': (c_int, [ctypes.POINTER(c_i64), c_i32, c_i32,
+                                           ctypes.POINTER(c_p)]),
+    'pmx_workspace_slots': (c_int, [c_p, ctypes.POINTER(c_i32)]),
+    'pmx_nbody_steps_batch': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_i32,
+                                      ctypes.POINTER(PmxSim), c_i32, c_i32, c_p]),
+    'pmx_nbody_adj_steps_batch': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_i32,
+                                          ctypes.POINTER(PmxSim), c_i32, c_i32, c_p]),
     'pmx_force': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_p, c_p, c_i64, c_i64, c_d, c_p, c_p]),
     'pmx_force_vjp': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_p, c_p, c_i64, c_i64, c_d, c_p,
                               c_p, c_p, c_p, c_p]),
@@ -158,15 +173,17 @@ def stream_ptr(device=None):
     return c_p(torch.cuda.current_stream(device).cuda_stream)
 
 
-def make_spec(dim, wrap_shape, mesh_shape, conf_cell_size, offset=0, cell_size=None):
+def make_spec(dim, wrap_shape, mesh_shape, conf_cell_size, offset=0, cell_size=None, drop=True):
+    """``pmx_enmesh_spec``; ``wrap_shape=None``: no periodic wrapping."""
     s = EnmeshSpec()
     s.dim = dim
+    s.drop = int(bool(drop))
     off = offset
     if not hasattr(off, '__len__'):
         off = (float(off),) * dim
     off = [float(x) for x in off]
     for a in range(3):
-        s.wrap_shape[a] = int(wrap_shape[a]) if a < dim else 1
+        s.wrap_shape[a] = (0 if wrap_shape is None else int(wrap_shape[a])) if a < dim else 1
         s.mesh_shape[a] = int(mesh_shape[a]) if a < dim else 1
         s.offset[a] = off[a] if a < dim else 0.0
     s.conf_cell_size = float(conf_cell_size)
@@ -178,13 +195,16 @@ class Workspace:
     """Owner of a ``pmx_workspace`` (mesh buffers, spectra, cuFFT plans)."""
 
     def __init__(self, mesh_shape, adjoint=True, device=None, cufft3d=False, window=False,
-                 plane=False, vec=False, graphs=True, plane16=False, chains=0, slab_log2=0):
+                 plane=False, vec=False, graphs=True, plane16=False, chains=0, slab_log2=0,
+                 slots=1):
         """Flags of pmx_workspace_create (include/pmx.h): ``cufft3d`` 3-D
         cuFFT plans instead of the fused x pass, ``window`` warp-window
         deposits, ``plane`` cluster plane kernels (``plane16``: clusters of
         16), ``vec`` vector z-pair reductions, ``graphs`` slab loops as CUDA
         graphs, ``chains`` concurrent slab chains and ``slab_log2`` planes
-        per cuFFT execution (0: defaults)."""
+        per cuFFT execution (0: defaults).  ``slots`` > 1: a batched
+        workspace for that many simulations of this mesh shape
+        (pmx_workspace_create_batch)."""
         load()
         self.mesh_shape = tuple(int(s) for s in mesh_shape)
         self.adjoint = adjoint
@@ -197,8 +217,14 @@ class Workspace:
         self.device = torch.device('cuda', torch.cuda.current_device() if device is None else device)
         shp = (c_i64 * 3)(*self.mesh_shape)
         h = c_p()
+        self.slots = int(slots)
         with torch.cuda.device(self.device):
-            check(_lib.pmx_workspace_create(shp, flags, ctypes.byref(h)), 'pmx_workspace_create')
+            if self.slots == 1:
+                check(_lib.pmx_workspace_create(shp, flags, ctypes.byref(h)),
+                      'pmx_workspace_create')
+            else:
+                check(_lib.pmx_workspace_create_batch(shp, flags, self.slots, ctypes.byref(h)),
+                      'pmx_workspace_create_batch')
         self.handle = h
 
     def __del__(self):

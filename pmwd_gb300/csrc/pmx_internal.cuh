@@ -52,7 +52,8 @@ inline int stride_grid(int64_t work, int threads, int per_sm = 8) {
 struct EmParams {
     int dim;           // user spatial dims
     int pad;           // 3 - dim: internal axes [0, pad) are singleton
-    int wrap[3];       // s1 per internal axis
+    int wrap[3];       // s1 per internal axis (0: no wrapping, s1 = None)
+    int drop;          // without wrapping: negative indices -> s2
     int64_t shape[3];  // s2 per internal axis
     int64_t stride[3]; // mesh cell stride per internal axis
     int f64;           // 1: non-default (float64) branch, pm_util.py:99-118
@@ -150,22 +151,29 @@ __device__ __forceinline__ void enmesh_axis(const EmParams &p, int a, int pm, fl
             float d2 = __fsub_rn(x, (float)ii);
             ax.w[nb] = __fsub_rn(1.f, fabsf(d2));
             ax.s[nb] = sgnf(-d2);
-            ax.i[nb] = pymod(ii + ip, p.wrap[a]);
+            // without wrapping, the reference's int16 sum (two's complement)
+            ax.i[nb] = p.wrap[a] ? pymod(ii + ip, p.wrap[a]) : (int)(short)(ii + ip);
         }
     } else {
         double P = __dsub_rn(__dadd_rn(__dmul_rn((double)pm, p.a1d), (double)d), p.b12[a]);
 #pragma unroll
         for (int nb = 0; nb < 2; ++nb) {
             double x = nb ? __dadd_rn(P, p.a2d) : P;
-            x = pyfmod(x, p.L[a]);
+            if (p.wrap[a]) x = pyfmod(x, p.L[a]);
             double q = floordiv(x, p.a2d);
             double d2 = __dsub_rn(P, __dmul_rn(q, p.a2d));
-            d2 = __dsub_rn(d2, __dmul_rn(rint(__ddiv_rn(d2, p.L[a])), p.L[a]));
+            if (p.wrap[a]) d2 = __dsub_rn(d2, __dmul_rn(rint(__ddiv_rn(d2, p.L[a])), p.L[a]));
             float d2f = __fdiv_rn((float)d2, p.a2f);
             ax.w[nb] = __fsub_rn(1.f, fabsf(d2f));
             ax.s[nb] = sgnf(-d2f);
             ax.i[nb] = (int)(short)(int)q;
         }
+    }
+    // pm_util.py:139-140: without wrapping, negative indices are set to s2
+    if (!p.wrap[a] && p.drop) {
+#pragma unroll
+        for (int nb = 0; nb < 2; ++nb)
+            if (ax.i[nb] < 0) ax.i[nb] = (int)p.shape[a];
     }
 }
 

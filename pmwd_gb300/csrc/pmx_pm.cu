@@ -62,13 +62,21 @@ int make_em_params(const pmx_enmesh_spec *s, EmParams *p) {
     if (!(s->conf_cell_size > 0)) return fail(PMX_ERR_ARG, "conf_cell_size must be > 0");
     p->dim = s->dim;
     p->pad = 3 - s->dim;
+    // all wrap_shape entries 0: no periodic wrapping (s1 = None)
+    bool nowrap = true;
+    for (int u = 0; u < s->dim; ++u) nowrap = nowrap && s->wrap_shape[u] == 0;
+    p->drop = nowrap && s->drop;
     for (int a = 0; a < 3; ++a) {
         int u = a - p->pad;
         if (u < 0) {
             p->wrap[a] = 1;
             p->shape[a] = 1;
+        } else if (nowrap) {
+            if (s->mesh_shape[u] <= 0) return fail(PMX_ERR_ARG, "mesh_shape must be > 0");
+            p->wrap[a] = 0;
+            p->shape[a] = s->mesh_shape[u];
         } else {
-            if (s->wrap_shape[u] <= 0) return fail(PMX_ERR_ARG, "wrap_shape must be > 0");
+            if (s->wrap_shape[u] <= 0) return fail(PMX_ERR_ARG, "wrap_shape must be > 0 (or all 0)");
             if (s->mesh_shape[u] <= 0) return fail(PMX_ERR_ARG, "mesh_shape must be > 0");
             p->wrap[a] = s->wrap_shape[u];
             p->shape[a] = s->mesh_shape[u];
@@ -270,7 +278,7 @@ using namespace pmx;
 // C ABI
 // ---------------------------------------------------------------------------
 
-extern "C" int pmx_version(void) { return 100; }
+extern "C" int pmx_version(void) { return 200; }
 
 extern "C" const char *pmx_last_error(void) { return g_err.c_str(); }
 

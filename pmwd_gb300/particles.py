@@ -115,15 +115,16 @@ def ptcl_enmesh(ptcl, conf, offset=0, cell_size=None, mesh_shape=None, wrap=True
     """Multilinear mesh indices, fractions and fraction gradients
     (particles.py:212-254) computed by the CUDA ``pmx_enmesh`` kernel.
 
-    Only ``wrap=True`` is supported (the periodic case scatter and gather
-    use); with wrapping no index is negative, so ``drop`` has no effect.
+    ``wrap``: wrap around the periodic boundaries (``conf.mesh_shape``);
+    without wrapping the indices are the reference's int16 sums, and with
+    ``drop`` the negative ones are replaced by ``mesh_shape`` (with wrapping
+    no index is negative, so ``drop`` has no effect).
     """
-    if not wrap:
-        raise NotImplementedError('wrap=False is not supported by the GPU enmesh')
     if mesh_shape is None:
         mesh_shape = conf.mesh_shape
     n, dim = ptcl.pmid.shape
-    spec = _lib.make_spec(dim, conf.mesh_shape, mesh_shape, conf.cell_size, offset, cell_size)
+    spec = _lib.make_spec(dim, conf.mesh_shape if wrap else None, mesh_shape, conf.cell_size,
+                          offset, cell_size, drop=drop)
     dev = ptcl.disp.device
     nk = 2 ** dim
     ind = torch.empty((n, nk, dim), dtype=torch.int32, device=dev)

@@ -44,9 +44,9 @@ def ptcl_case(conf, std, seed=0, edge=False):
     return pmid, disp
 
 
-def enmesh_gpu(dev, dim, wrap, shape, cell, pmid, disp, offset=0, cell_size=None):
+def enmesh_gpu(dev, dim, wrap, shape, cell, pmid, disp, offset=0, cell_size=None, drop=True):
     n = len(pmid)
-    spec = _lib.make_spec(dim, wrap, shape, cell, offset, cell_size)
+    spec = _lib.make_spec(dim, wrap, shape, cell, offset, cell_size, drop=drop)
     nk = 2 ** dim
     ind = torch.empty((n, nk, dim), dtype=torch.int32, device=dev)
     frac = torch.empty((n, nk), dtype=torch.float32, device=dev)
@@ -91,6 +91,45 @@ def test_enmesh_low_dim_bit_exact(cuda, dim):
         np.testing.assert_array_equal(i_g, i_o.astype(np.int32))
         np.testing.assert_array_equal(f_g, f_o)
         np.testing.assert_array_equal(g_g, g_o)
+
+
+@pytest.mark.parametrize('offset, cell_size', [(0, None), (0.3, None), ((0.1, -2.7, 5.0), None),
+                                               (0, 'half'), (0.6, 'ratio')])
+@pytest.mark.parametrize('drop', [True, False])
+def test_enmesh_without_wrapping_bit_exact(cuda, offset, cell_size, drop):
+    """particles.py:212-254 with wrap=False (s1 = None, pm_util.py:139-140):
+    no periodic wrapping; particles displaced past both edges give negative
+    indices (replaced by s2 when drop) and indices >= s2."""
+    conf = oc.OConf(2.0, (8, 6, 10), 2, float_dtype=np.float32)
+    if cell_size == 'half':
+        cell_size = conf.cell_size / 2
+    elif cell_size == 'ratio':
+        cell_size = conf.cell_size * 0.7
+    pmid, disp = ptcl_case(conf, 3.0 * conf.cell_size, edge=True)
+    shape = conf.mesh_shape if cell_size is None else tuple(2 * s for s in conf.mesh_shape)
+    i_o, f_o, g_o = pm.enmesh(pmid, disp, conf.cell_size, None, offset, cell_size,
+                              shape if drop else None, True)
+    assert (i_o < 0).any() != drop and (i_o >= np.array(shape)).any()
+    i_g, f_g, g_g = enmesh_gpu(cuda, 3, None, shape, conf.cell_size, pmid, disp, offset,
+                               cell_size, drop=drop)
+    np.testing.assert_array_equal(i_g, i_o.astype(np.int32))
+    np.testing.assert_array_equal(f_g, f_o)
+    np.testing.assert_array_equal(g_g, g_o)
+
+
+def test_ptcl_enmesh_wrap_false(cuda):
+    """The public ptcl_enmesh with wrap=False (and drop) against the oracle."""
+    conf = oc.OConf(1.0, (8, 8, 8), 1, float_dtype=np.float32)
+    gconf = pg.Configuration(1.0, (8, 8, 8), 1)
+    pmid, disp = ptcl_case(conf, 2.0, edge=True)
+    ptcl = pg.Particles(gconf, T(pmid, cuda), T(disp, cuda))
+    for drop in (True, False):
+        ind, frac, fg = pg.ptcl_enmesh(ptcl, gconf, wrap=False, drop=drop, grad=True)
+        i_o, f_o, g_o = pm.enmesh(pmid, disp, conf.cell_size, None, 0, None,
+                                  conf.mesh_shape if drop else None, True)
+        np.testing.assert_array_equal(ind.cpu().numpy(), i_o)
+        np.testing.assert_array_equal(frac.cpu().numpy(), f_o)
+        np.testing.assert_array_equal(fg.cpu().numpy(), g_o)
 
 
 def _spec_for(conf, mesh, dim, offset, cell_size):
