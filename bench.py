@@ -53,6 +53,9 @@ def parse():
     ap.add_argument('--nbody-steps', type=int, default=100)
     ap.add_argument('--cpu-sample', type=int, default=48,
                     help='particle grid side of the bounded CPU sample')
+    ap.add_argument('--deposit', default='atomic', choices=['atomic', 'agg', 'window'],
+                    help='CIC deposits: one float32 reduction per contribution, warp-aggregated '
+                         'for particles sharing a cell, or per-warp shared-memory windows')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-full-run', action='store_true',
@@ -264,6 +267,7 @@ def workload_config(args, world):
                         f'K forward leapfrog steps then their K reversible-adjoint steps of a '
                         f'{args.nbody_steps}-step run (rates per fwd+adj step pair)',
             'ptcl': side ** 3, 'mesh_cells': mside ** 3, 'parallelism': f'replicas x{world}',
+            'deposit': args.deposit,
             'l2': 'inputs larger than L2 (mesh 4.3 GB per array)'}
 
 
@@ -346,7 +350,8 @@ def run_pmx(args, rank, world, local_rank):
     f_adj = (_lib.c_f * 3)(*adj32[-1])
     Om = float(cosmo.Omega_m)
 
-    ws = _lib.workspace(conf.mesh_shape, adjoint=True)
+    ws = _lib.Workspace(conf.mesh_shape, adjoint=True, agg=args.deposit == 'agg',
+                        window=args.deposit == 'window')
     spec = _lib.make_spec(3, conf.mesh_shape, conf.mesh_shape, conf.cell_size)
     dots = torch.zeros(4, dtype=torch.float64, device=dev)
     P = _lib.ptr
@@ -689,8 +694,35 @@ def run_contention(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
+    # the force VJP (density deposit, gather VJP with its 24 reductions per
+    # particle, scatter VJP), through plain atomics and warp windows
+    ws_win = _lib.Workspace(conf.mesh_shape, adjoint=True, window=True)
+    ws_agg = _lib.Workspace(conf.mesh_shape, adjoint=True, agg=True)
+    cot = torch.randn((N, 3), dtype=torch.float32, device=dev,
+                      generator=torch.Generator(device=dev).manual_seed(5))
+    dcot = torch.empty_like(cot)
+    om_cot = torch.zeros((), dtype=torch.float64, device=dev)
+
+    def vjp_stages(w, d, reps=5):
+        def fv():
+            _lib.check(lib.pmx_force_vjp(w.handle, spec, P(pmid), P(d), N, N, Om, P(cot), P(acc),
+                                         P(dcot), P(om_cot), stream), 'pmx_force_vjp')
+        for _ in range(2):
+            fv()
+        torch.cuda.synchronize()
+        _lib.profile_read(w)
+        lib.pmx_profile_enable(w.handle, 1)
+        t = timed(fv, reps)
+        lib.pmx_profile_enable(w.handle, 0)
+        st, _ = _lib.profile_read(w)
+        return {'force_vjp_ms': t,
+                'deposit_ms': st['deposit_fwd'][0] / max(st['deposit_fwd'][1], 1),
+                'gather3_adj_ms': st['gather3_adj'][0] / max(st['gather3_adj'][1], 1)}
+
     res = {}
     for name, d in (('clustered', disp), ('lattice', torch.zeros_like(disp))):
+        res[name] = {'vjp_atomics': vjp_stages(ws, d), 'vjp_windows': vjp_stages(ws_win, d),
+                     'vjp_aggregated': vjp_stages(ws_agg, d)}
         def sc():
             mesh.zero_()
             _lib.check(lib.pmx_scatter(spec, P(pmid), P(d), N, None, val, 1, P(mesh), stream),
@@ -705,8 +737,8 @@ def run_contention(args):
         sc()
         torch.cuda.synchronize()
         peak = float(mesh.max()) / val  # particles (CIC weight) in the fullest cell
-        res[name] = {'scatter_ms': timed(sc, 10) - t_zero, 'force_ms': timed(fo, 5),
-                     'gather3_ms': timed(ga, 10), 'max_ptcl_per_cell': peak}
+        res[name].update({'scatter_ms': timed(sc, 10) - t_zero, 'force_ms': timed(fo, 5),
+                          'gather3_ms': timed(ga, 10), 'max_ptcl_per_cell': peak})
         for k in ('scatter', 'gather3'):
             res[name][k + '_ptcl_per_s'] = N / (res[name][k + '_ms'] / 1e3)
     line = {'metric': 'scatter/gather contention (C3)', 'unit': 'ms',

@@ -134,6 +134,10 @@ typedef struct pmx_workspace pmx_workspace;
                               directly instead of replaying captured graphs */
 #define PMX_WS_PLANE16 64  /* plane kernels in clusters of 16 CTAs (the
                               non-portable size) instead of 8 */
+#define PMX_WS_AGG 128     /* warp-aggregated deposits: lanes whose particles
+                              share a cell sum their contributions in shared
+                              memory and one lane issues the reductions
+                              (helps clustered late-time states) */
 /* Slab-wise plane transforms: number of concurrent chains (1..4; 0 = the
  * default 2) and log2 of the x-planes per cuFFT execution (1..15; 0 = the
  * default, the smallest power of two >= 8 reaching 32 MB), packed into the

@@ -115,6 +115,7 @@ PMX_WS_PLANE = 8
 PMX_WS_VEC = 16
 PMX_WS_NO_GRAPH = 32
 PMX_WS_PLANE16 = 64
+PMX_WS_AGG = 128
 PMX_WS_CHAINS_SHIFT = 8
 PMX_WS_SLAB_SHIFT = 12
 
@@ -196,11 +197,12 @@ class Workspace:
 
     def __init__(self, mesh_shape, adjoint=True, device=None, cufft3d=False, window=False,
                  plane=False, vec=False, graphs=True, plane16=False, chains=0, slab_log2=0,
-                 slots=1):
+                 slots=1, agg=False):
         """Flags of pmx_workspace_create (include/pmx.h): ``cufft3d`` 3-D
         cuFFT plans instead of the fused x pass, ``window`` warp-window
         deposits, ``plane`` cluster plane kernels (``plane16``: clusters of
-        16), ``vec`` vector z-pair reductions, ``graphs`` slab loops as CUDA
+        16), ``vec`` vector z-pair reductions, ``agg`` warp-aggregated
+        deposits, ``graphs`` slab loops as CUDA
         graphs, ``chains`` concurrent slab chains and ``slab_log2`` planes
         per cuFFT execution (0: defaults).  ``slots`` > 1: a batched
         workspace for that many simulations of this mesh shape
@@ -211,7 +213,7 @@ class Workspace:
         flags = ((PMX_WS_ADJOINT if adjoint else 0) | (PMX_WS_CUFFT3D if cufft3d else 0)
                  | (PMX_WS_WINDOW if window else 0) | (PMX_WS_PLANE if plane else 0)
                  | (PMX_WS_VEC if vec else 0) | (0 if graphs else PMX_WS_NO_GRAPH)
-                 | (PMX_WS_PLANE16 if plane16 else 0)
+                 | (PMX_WS_PLANE16 if plane16 else 0) | (PMX_WS_AGG if agg else 0)
                  | ((int(chains) & 7) << PMX_WS_CHAINS_SHIFT)
                  | ((int(slab_log2) & 15) << PMX_WS_SLAB_SHIFT))
         self.device = torch.device('cuda', torch.cuda.current_device() if device is None else device)

@@ -32,6 +32,7 @@ using namespace pmx;
 namespace {
 
 constexpr int PMAX = 4096;       // max blocks of a particle kernel (partials per slot)
+constexpr int BMAX = 16;         // most simulations of one batched call
 constexpr int NSLOT = 4;         // dot-product slots
 constexpr int PT = 256;          // threads per particle kernel
 constexpr double PI = 3.141592653589793;
@@ -64,24 +65,31 @@ namespace slabs {
 constexpr int KMAX = 4;  // most concurrent slab chains
 // One slab-wise 2-D transform: a cuFFT plan (with its own work area) per
 // chain, and the captured graph of the whole slab loop.
+constexpr int GMAX = 16;  // captured slab graphs per transform (one per slot count)
 struct SlabXf {
     cufftHandle plan[KMAX] = {};
     bool have[KMAX] = {};
     void *work[KMAX] = {};
     bool r2c = true;
-    cudaGraphExec_t exec = nullptr;
-    const void *in = nullptr;   // buffers the graph was captured with
-    void *out = nullptr;
+    // the captured slab loop of each slot count (1..GMAX), with the buffers
+    // it was captured with
+    cudaGraphExec_t exec[GMAX + 1] = {};
+    const void *in[GMAX + 1] = {};
+    void *out[GMAX + 1] = {};
 };
 }  // namespace slabs
 }  // namespace pmx
 using pmx::slabs::SlabXf;
 using pmx::slabs::KMAX;
+using pmx::slabs::GMAX;
 
 struct pmx_workspace {
     int dev = 0;
     int flags = 0;
     int64_t n0 = 0, n1 = 0, n2 = 0, n2h = 0, M = 0, Mc = 0;
+    // simulations one call can carry (batched workspaces): every mesh
+    // buffer below holds `slots` consecutive copies, slot-major
+    int slots = 1;
     float *dens = nullptr;
     float2 *ck = nullptr;
     float *g = nullptr;
@@ -104,6 +112,7 @@ struct pmx_workspace {
     bool plane = false;
     bool plane16 = false;       // clusters of 16 CTAs instead of 8
     bool vec = false;           // vector z-pair reductions (n2 % 4 == 0)
+    bool agg = false;           // warp-aggregated deposits
     float2 *ptw = nullptr;      // plane_twiddles(n1, n2)
     float2 *pscr = nullptr;     // c2r scratch: one n1 x n2p plane per cluster
     int pcl = 0;                // clusters the scratch serves
@@ -116,10 +125,11 @@ struct pmx_workspace {
     cudaStream_t cap = nullptr, aux[KMAX] = {};
     cudaEvent_t fork = nullptr, join[KMAX] = {};
     // the adjoint's density cotangent (rho_cot), in g behind the complex
-    // spectrum the last inverse transform reads: the density itself stays
-    // free, so a multi-step run can deposit the next step's density while
-    // it gathers rho_cot
-    float *rcot = nullptr;
+    // spectra the last inverse transform reads (b slots of n0 n1 n2p
+    // complex values for a call over b slots, then b meshes): the density
+    // itself stays free, so a multi-step run can deposit the next step's
+    // density while it gathers rho_cot
+    float *rcot_of(int b) const { return g + 2 * b * n0 * n1 * n2p; }
     // stage profiler: CUDA events around every stage while enabled
     bool prof_on = false;
     struct Rec {
@@ -312,6 +322,8 @@ struct Hot {
     // n2 % 4 == 0: every mesh row starts on 16 bytes, so z-neighbour pairs
     // inside one aligned group of four floats take one vector reduction
     bool vec;
+    // warp-aggregated deposits (mesh indices below 2^32 - 32)
+    bool agg;
 };
 
 __device__ __forceinline__ void hot_axis(const Hot &h, int a, int pm, float d, Axis &ax) {
@@ -404,6 +416,92 @@ __device__ __forceinline__ void hot_deposit(const Hot &h, const Axis ax[3], floa
                   __fmul_rn(h.val, __fmul_rn(fxy, ax[2].w[0])),
                   __fmul_rn(h.val, __fmul_rn(fxy, ax[2].w[1])), h.vec);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-aggregated deposits for clustered particles.  Two particles with the
+// same base cell (the wrapped lower neighbour on every axis) share all eight
+// neighbour cells.  A warp first matches its lanes' base cells; when no two
+// lanes share one (the nearly uniform early steps) it deposits directly,
+// as hot_deposit.  Otherwise every lane adds its NC x 8 contributions into a
+// shared-memory slot of its group's lowest lane, and that lane issues one
+// global reduction per cell and component for the whole group: in a halo,
+// where many particles of a warp fall into the same cell, the contended L2
+// reductions drop by the group size.  Only the order of the float32 sums
+// changes.  Needs a warp-uniform loop (every lane calls it) and mesh
+// indices below 2^32 - 32 (Hot::agg).
+// ---------------------------------------------------------------------------
+
+constexpr int AGG_SLOT = 8;  // floats per lane and component in the warp buffer
+
+// Adds s[c] * frac_k to component c of neighbour k for NC components:
+// component c of cell (row, z) at base + row + z + c * cs, the row of
+// neighbour pair p at hot_row(h, ax, p) + x_p * xs.
+template <int NC>
+__device__ __forceinline__ void agg_deposit(const Hot &h, bool act, const Axis ax[3],
+                                            const float s[NC], float *base, int64_t xs,
+                                            int64_t cs, float *wbuf) {
+    const int lane = threadIdx.x & 31;
+    const unsigned key =
+        act ? (unsigned)((int64_t)ax[0].i[0] * h.stride[0] + (int64_t)ax[1].i[0] * h.stride[1] +
+                         ax[2].i[0])
+            : 0xFFFFFFFFu - (unsigned)lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (!__any_sync(0xffffffffu, (peers & (peers - 1)) != 0)) {   // no shared base cell
+        if (act) {
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                const float fxy = __fmul_rn(ax[0].w[p & 1], ax[1].w[(p >> 1) & 1]);
+                const float fa = __fmul_rn(fxy, ax[2].w[0]), fb = __fmul_rn(fxy, ax[2].w[1]);
+                float *row = base + hot_row(h, ax, p) + (int64_t)ax[0].i[p & 1] * xs;
+#pragma unroll
+                for (int c = 0; c < NC; ++c)
+                    zpair_add(row + c * cs, ax[2].i[0], ax[2].i[1], __fmul_rn(s[c], fa),
+                              __fmul_rn(s[c], fb), h.vec);
+            }
+        }
+        return;
+    }
+    const int leader = __ffs(peers) - 1;
+    float *slot = wbuf + leader * (AGG_SLOT * NC);
+    if (act) {
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            const float fxy = __fmul_rn(ax[0].w[p & 1], ax[1].w[(p >> 1) & 1]);
+            const float fa = __fmul_rn(fxy, ax[2].w[0]), fb = __fmul_rn(fxy, ax[2].w[1]);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                atomicAdd(slot + (2 * p) * NC + c, __fmul_rn(s[c], fa));
+                atomicAdd(slot + (2 * p + 1) * NC + c, __fmul_rn(s[c], fb));
+            }
+        }
+    }
+    __syncwarp();
+    if (act && lane == leader) {
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            float *row = base + hot_row(h, ax, p) + (int64_t)ax[0].i[p & 1] * xs;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                float *a = slot + (2 * p) * NC + c, *b = slot + (2 * p + 1) * NC + c;
+                zpair_add(row + c * cs, ax[2].i[0], ax[2].i[1], *a, *b, h.vec);
+                *a = 0.f;
+                *b = 0.f;
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// This warp's zeroed aggregation buffer (32 lanes x 8 neighbours x NC).
+template <int NC>
+__device__ __forceinline__ float *agg_buffer() {
+    __shared__ float buf[PT / 32][32 * AGG_SLOT * NC];
+    float *w = buf[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < 32 * AGG_SLOT * NC; i += 32) w[i] = 0.f;
+    __syncwarp();
+    return w;
 }
 
 // ---------------------------------------------------------------------------
@@ -507,14 +605,16 @@ __device__ __forceinline__ void win_zero(float *buf, int nfloats) {
 // WIN: deposit through the warp windows; KAHAN: compensated updates (the
 // compensation arrays in h are then non-NULL).  Both are template arguments
 // so the default path carries neither their registers nor their branches.
-template <bool KD, bool WIN, bool KAHAN>
-__global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ pmid, float *disp,
+template <bool KD, bool WIN, bool KAHAN, bool AGG = false>
+__device__ __forceinline__ void kds_body(Hot h, const int16_t *__restrict__ pmid, float *disp,
                                             float *vel, const float *__restrict__ acc, int64_t n,
                                             float K1, float D, float *dens) {
     extern __shared__ __align__(16) float wsm[];
     const int lane = threadIdx.x & 31;
     float *buf = wsm + (threadIdx.x >> 5) * (WROWS * WZ);
     float *const vcomp = KAHAN ? h.vcomp : nullptr, *const dcomp = KAHAN ? h.dcomp : nullptr;
+    float *abuf = nullptr;
+    if constexpr (AGG) abuf = agg_buffer<1>();
     if (WIN) win_zero(buf, WROWS * WZ);
     __syncwarp();
     // warp-uniform loop: each warp takes 32 consecutive particles
@@ -533,6 +633,11 @@ __global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ p
             }
             hot_enmesh(h, pmid, q, d, ax);
         }
+        if constexpr (AGG) {
+            const float sv[1] = {h.val};
+            agg_deposit<1>(h, act, ax, sv, dens, 0, 0, abuf);
+            continue;
+        }
         if (!WIN) {
             if (act) hot_deposit(h, ax, dens);
             continue;
@@ -549,9 +654,16 @@ __global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ p
     }
 }
 
+template <bool KD, bool WIN, bool KAHAN, bool AGG = false>
+__global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ pmid, float *disp,
+                                            float *vel, const float *__restrict__ acc, int64_t n,
+                                            float K1, float D, float *dens) {
+    kds_body<KD, WIN, KAHAN, AGG>(h, pmid, disp, vel, acc, n, K1, D, dens);
+}
+
 // Forward: gather the three acceleration meshes, optionally kick with K2.
 template <bool KICK, bool KAHAN>
-__global__ void __launch_bounds__(PT) k_gather3(Hot h, const int16_t *__restrict__ pmid,
+__device__ __forceinline__ void gather3_body(Hot h, const int16_t *__restrict__ pmid,
                                                 const float *__restrict__ disp, float *vel,
                                                 float *acc, int64_t n, int64_t M,
                                                 const float *__restrict__ g, float K2) {
@@ -575,11 +687,19 @@ __global__ void __launch_bounds__(PT) k_gather3(Hot h, const int16_t *__restrict
     }
 }
 
+template <bool KICK, bool KAHAN>
+__global__ void __launch_bounds__(PT) k_gather3(Hot h, const int16_t *__restrict__ pmid,
+                                                const float *__restrict__ disp, float *vel,
+                                                float *acc, int64_t n, int64_t M,
+                                                const float *__restrict__ g, float K2) {
+    gather3_body<KICK, KAHAN>(h, pmid, disp, vel, acc, n, M, g, K2);
+}
+
 // Adjoint: kick_adj(K1) then drift_adj(D) (nbody.py:80-99, 49-67), then the
 // density deposit of the reconstructed positions.  Partial dots:
 // slot 0 = sum(vel_cot*acc), slot 1 = sum(disp_cot*vel).
-template <bool KD, bool WIN, bool KAHAN>
-__global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pmid, float *disp,
+template <bool KD, bool WIN, bool KAHAN, bool AGG = false>
+__device__ __forceinline__ void ka_body(Hot h, const int16_t *__restrict__ pmid, float *disp,
                                            float *vel, const float *__restrict__ acc,
                                            float *disp_cot, float *vel_cot,
                                            const float *__restrict__ alpha, int64_t n, float K1,
@@ -589,6 +709,8 @@ __global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pm
     const int lane = threadIdx.x & 31;
     float *buf = wsm + (threadIdx.x >> 5) * (WROWS * WZ);
     float *const vcomp = KAHAN ? h.vcomp : nullptr, *const dcomp = KAHAN ? h.dcomp : nullptr;
+    float *abuf = nullptr;
+    if constexpr (AGG) abuf = agg_buffer<1>();
     if (WIN) win_zero(buf, WROWS * WZ);
     __syncwarp();
     double s0 = 0.0, s1 = 0.0;
@@ -615,6 +737,11 @@ __global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pm
             }
             hot_enmesh(h, pmid, q, d, ax);
         }
+        if constexpr (AGG) {
+            const float sv[1] = {h.val};
+            agg_deposit<1>(h, act, ax, sv, dens, 0, 0, abuf);
+            continue;
+        }
         if (!WIN) {
             if (act) hot_deposit(h, ax, dens);
             continue;
@@ -639,12 +766,22 @@ __global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pm
     }
 }
 
+template <bool KD, bool WIN, bool KAHAN, bool AGG = false>
+__global__ void __launch_bounds__(PT) k_ka(Hot h, const int16_t *__restrict__ pmid, float *disp,
+                                           float *vel, const float *__restrict__ acc,
+                                           float *disp_cot, float *vel_cot,
+                                           const float *__restrict__ alpha, int64_t n, float K1,
+                                           float D, float *dens, double *part) {
+    ka_body<KD, WIN, KAHAN, AGG>(h, pmid, disp, vel, acc, disp_cot, vel_cot, alpha, n, K1, D, dens,
+                                 part);
+}
+
 // Adjoint: gather the three acceleration meshes (new acc), the gather VJP
 // disp_cot term sum_j vc_j sum_k g_j[k] dfrac_k / cell (into alpha), and the
 // gather VJP mesh term mcot_j[k] += vc_j frac_k.  Partial dot slot 2 =
 // sum(vel_cot * acc_new).
-template <bool WIN>
-__global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__ pmid,
+template <bool WIN, bool AGG = false>
+__device__ __forceinline__ void g3adj_body(Hot h, const int16_t *__restrict__ pmid,
                                               const float *__restrict__ disp,
                                               const float *__restrict__ vel_cot, float *acc,
                                               float *alpha, int64_t n, int64_t M,
@@ -654,6 +791,8 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
     extern __shared__ __align__(16) float wsm[];
     const int lane = threadIdx.x & 31;
     float *buf = wsm + (threadIdx.x >> 5) * (3 * WROWS * WZ);
+    float *abuf = nullptr;
+    if constexpr (AGG) abuf = agg_buffer<3>();
     if (WIN) win_zero(buf, 3 * WROWS * WZ);
     __syncwarp();
     double s2 = 0.0;
@@ -685,7 +824,7 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
                 c1 = __fadd_rn(c1, __fmul_rn(t, fg[1]));
                 c2 = __fadd_rn(c2, __fmul_rn(t, fg[2]));
             }
-            if (!WIN) {
+            if (!WIN && !AGG) {
                 // gather-VJP mesh term mcot_j[k] += vc_j frac_k
 #pragma unroll
                 for (int p = 0; p < 4; ++p) {
@@ -704,6 +843,11 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
             st3(alpha, q, make_float3(__fdiv_rn(c0, h.cell), __fdiv_rn(c1, h.cell),
                                       __fdiv_rn(c2, h.cell)));
             s2 += dot3d(vc, a);
+        }
+        if constexpr (AGG) {
+            const float sv[3] = {vc.x, vc.y, vc.z};
+            agg_deposit<3>(h, act, ax, sv, mcot, h.gxs, h.gjs, abuf);
+            continue;
         }
         if (!WIN) continue;
         // gather-VJP mesh term through the warp window, three components
@@ -726,11 +870,21 @@ __global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__
     if (threadIdx.x == 0) part[2 * PMAX + blockIdx.x] = t2;
 }
 
+template <bool WIN, bool AGG = false>
+__global__ void __launch_bounds__(PT) k_g3adj(Hot h, const int16_t *__restrict__ pmid,
+                                              const float *__restrict__ disp,
+                                              const float *__restrict__ vel_cot, float *acc,
+                                              float *alpha, int64_t n, int64_t M,
+                                              const float *__restrict__ g, float *mcot,
+                                              double *part) {
+    g3adj_body<WIN, AGG>(h, pmid, disp, vel_cot, acc, alpha, n, M, g, mcot, part);
+}
+
 // Adjoint: scatter VJP disp_cot term sum_k (rho_cot[k] val) dfrac_k / cell
 // added into alpha, then optionally kick_adj(K2): vel += acc*K2,
 // disp_cot -= alpha*K2.
 template <bool KICK, bool KAHAN>
-__global__ void __launch_bounds__(PT) k_sadj(Hot h, const int16_t *__restrict__ pmid,
+__device__ __forceinline__ void sadj_body(Hot h, const int16_t *__restrict__ pmid,
                                              const float *__restrict__ disp, float *vel,
                                              const float *__restrict__ acc, float *disp_cot,
                                              float *alpha, int64_t n,
@@ -762,6 +916,15 @@ __global__ void __launch_bounds__(PT) k_sadj(Hot h, const int16_t *__restrict__ 
     }
 }
 
+template <bool KICK, bool KAHAN>
+__global__ void __launch_bounds__(PT) k_sadj(Hot h, const int16_t *__restrict__ pmid,
+                                             const float *__restrict__ disp, float *vel,
+                                             const float *__restrict__ acc, float *disp_cot,
+                                             float *alpha, int64_t n,
+                                             const float *__restrict__ rho_cot, float K2) {
+    sadj_body<KICK, KAHAN>(h, pmid, disp, vel, acc, disp_cot, alpha, n, rho_cot, K2);
+}
+
 // ---------------------------------------------------------------------------
 // Kernels that join two consecutive steps of a multi-step run: the last
 // particle pass of step i and the first of step i+1 have no FFT between them,
@@ -773,12 +936,12 @@ __global__ void __launch_bounds__(PT) k_sadj(Hot h, const int16_t *__restrict__ 
 // k_gather3<true> of step i, then k_kds<true> of step i+1: gather, kick K2,
 // kick K1n, drift Dn, deposit.  acc is not stored: the next force rewrites it
 // before anything reads it.
-__global__ void __launch_bounds__(PT) k_gk_kds(Hot h, const int16_t *__restrict__ pmid, float *disp,
-                                               float *vel, int64_t n, const float *__restrict__ g,
-                                               float K2, float K1n, float Dn, float *dens) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        Axis ax[3];
+// One particle of k_gk_kds up to the deposit: ax holds its new neighbours.
+__device__ __forceinline__ void gk_kds_particle(const Hot &h, const int16_t *__restrict__ pmid,
+                                                float *disp, float *vel,
+                                                const float *__restrict__ g, float K2, float K1n,
+                                                float Dn, int64_t q, Axis ax[3]) {
+    {
         float3 d = ld3(disp, q);
         hot_enmesh(h, pmid, q, d, ax);
         float a0 = 0.f, a1 = 0.f, a2 = 0.f;
@@ -798,26 +961,53 @@ __global__ void __launch_bounds__(PT) k_gk_kds(Hot h, const int16_t *__restrict_
         st3(vel, q, v);
         st3(disp, q, d);
         hot_enmesh(h, pmid, q, d, ax);
-        hot_deposit(h, ax, dens);
     }
+}
+
+template <bool AGG = false>
+__device__ __forceinline__ void gk_kds_body(Hot h, const int16_t *__restrict__ pmid, float *disp,
+                                            float *vel, int64_t n, const float *__restrict__ g,
+                                            float K2, float K1n, float Dn, float *dens) {
+    if constexpr (!AGG) {
+        for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+             q += (int64_t)gridDim.x * blockDim.x) {
+            Axis ax[3];
+            gk_kds_particle(h, pmid, disp, vel, g, K2, K1n, Dn, q, ax);
+            hot_deposit(h, ax, dens);
+        }
+    } else {
+        float *abuf = agg_buffer<1>();
+        const float sv[1] = {h.val};
+        for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); q0 < n;
+             q0 += (int64_t)gridDim.x * blockDim.x) {   // warp-uniform
+            const int64_t q = q0 + (threadIdx.x & 31);
+            Axis ax[3];
+            if (q < n) gk_kds_particle(h, pmid, disp, vel, g, K2, K1n, Dn, q, ax);
+            agg_deposit<1>(h, q < n, ax, sv, dens, 0, 0, abuf);
+        }
+    }
+}
+
+template <bool AGG = false>
+__global__ void __launch_bounds__(PT) k_gk_kds(Hot h, const int16_t *__restrict__ pmid, float *disp,
+                                               float *vel, int64_t n, const float *__restrict__ g,
+                                               float K2, float K1n, float Dn, float *dens) {
+    gk_kds_body<AGG>(h, pmid, disp, vel, n, g, K2, K1n, Dn, dens);
 }
 
 // k_sadj<true> of adjoint step i, then k_ka<true> of adjoint step i+1: the
 // scatter-VJP term into alpha, kick_adj K2, kick_adj K1n, drift_adj Dn,
 // deposit; partial dots of step i+1 into slots 0, 1.  alpha is not stored:
 // the next gather VJP rewrites it before anything reads it.
-__global__ void __launch_bounds__(PT) k_sa_ka(Hot h, const int16_t *__restrict__ pmid,
-                                              float *disp, float *vel,
-                                              const float *__restrict__ acc, float *disp_cot,
-                                              float *vel_cot, const float *__restrict__ alpha,
-                                              int64_t n, const float *__restrict__ rho_cot,
-                                              float K2, float K1n, float Dn, float *dens,
-                                              double *part) {
-    __shared__ double sh[PT / 32];
-    double s0 = 0.0, s1 = 0.0;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        Axis ax[3];
+// One particle of k_sa_ka up to the deposit (dots into s0, s1).
+__device__ __forceinline__ void sa_ka_particle(const Hot &h, const int16_t *__restrict__ pmid,
+                                               float *disp, float *vel,
+                                               const float *__restrict__ acc, float *disp_cot,
+                                               float *vel_cot, const float *__restrict__ alpha,
+                                               const float *__restrict__ rho_cot, float K2,
+                                               float K1n, float Dn, int64_t q, Axis ax[3],
+                                               double &s0, double &s1) {
+    {
         float3 d = ld3(disp, q);
         hot_enmesh(h, pmid, q, d, ax);
         float c0 = 0.f, c1 = 0.f, c2 = 0.f;
@@ -850,7 +1040,39 @@ __global__ void __launch_bounds__(PT) k_sa_ka(Hot h, const int16_t *__restrict__
         st3(disp_cot, q, dc);
         st3(vel_cot, q, vc);
         hot_enmesh(h, pmid, q, d, ax);
-        hot_deposit(h, ax, dens);
+    }
+}
+
+template <bool AGG = false>
+__device__ __forceinline__ void sa_ka_body(Hot h, const int16_t *__restrict__ pmid,
+                                           float *disp, float *vel,
+                                           const float *__restrict__ acc, float *disp_cot,
+                                           float *vel_cot, const float *__restrict__ alpha,
+                                           int64_t n, const float *__restrict__ rho_cot,
+                                           float K2, float K1n, float Dn, float *dens,
+                                           double *part) {
+    __shared__ double sh[PT / 32];
+    double s0 = 0.0, s1 = 0.0;
+    if constexpr (!AGG) {
+        for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+             q += (int64_t)gridDim.x * blockDim.x) {
+            Axis ax[3];
+            sa_ka_particle(h, pmid, disp, vel, acc, disp_cot, vel_cot, alpha, rho_cot, K2, K1n,
+                           Dn, q, ax, s0, s1);
+            hot_deposit(h, ax, dens);
+        }
+    } else {
+        float *abuf = agg_buffer<1>();
+        const float sv[1] = {h.val};
+        for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); q0 < n;
+             q0 += (int64_t)gridDim.x * blockDim.x) {   // warp-uniform
+            const int64_t q = q0 + (threadIdx.x & 31);
+            Axis ax[3];
+            if (q < n)
+                sa_ka_particle(h, pmid, disp, vel, acc, disp_cot, vel_cot, alpha, rho_cot, K2,
+                               K1n, Dn, q, ax, s0, s1);
+            agg_deposit<1>(h, q < n, ax, sv, dens, 0, 0, abuf);
+        }
     }
     double t0 = block_sum<PT>(s0, sh);
     double t1 = block_sum<PT>(s1, sh);
@@ -858,6 +1080,18 @@ __global__ void __launch_bounds__(PT) k_sa_ka(Hot h, const int16_t *__restrict__
         part[0 * PMAX + blockIdx.x] = t0;
         part[1 * PMAX + blockIdx.x] = t1;
     }
+}
+
+template <bool AGG = false>
+__global__ void __launch_bounds__(PT) k_sa_ka(Hot h, const int16_t *__restrict__ pmid,
+                                              float *disp, float *vel,
+                                              const float *__restrict__ acc, float *disp_cot,
+                                              float *vel_cot, const float *__restrict__ alpha,
+                                              int64_t n, const float *__restrict__ rho_cot,
+                                              float K2, float K1n, float Dn, float *dens,
+                                              double *part) {
+    sa_ka_body<AGG>(h, pmid, disp, vel, acc, disp_cot, vel_cot, alpha, n, rho_cot, K2, K1n, Dn,
+                    dens, part);
 }
 
 // Sums the per-block partials in a fixed order: dots[s] = sum of slot s for
@@ -876,6 +1110,125 @@ __global__ void k_finish(const double *part, int nblk, double *dots, int nslots,
         if (threadIdx.x == 0) {
             if (dots && s < nslots) dots[s] = t;
             if (om_out && s == 2) *om_out = om_scale * t;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Batched simulations: one launch serves up to BMAX simulations that share a
+// mesh shape and cell size.  blockIdx.y selects the simulation; its particle
+// arrays, particle count, CIC value and this launch's leapfrog factors come
+// from a table passed by value (__grid_constant__: read in place from the
+// parameter space), its meshes are slot blockIdx.y of the workspace buffers.
+// Each body is the one the single-simulation kernels run, so a simulation's
+// arithmetic is the same alone and in a batch.
+// ---------------------------------------------------------------------------
+
+struct SimB {
+    const int16_t *pmid;
+    float *disp, *vel, *acc, *dcot, *vcot, *alpha;
+    int64_t n;
+    float val;     // f32(mesh_size / ptcl_num) of this simulation
+    float f[3];    // this launch's leapfrog factors (meaning per kernel)
+};
+struct BatchTab {
+    SimB s[BMAX];
+};
+
+// Slot b's share of a slot-major buffer of `per` elements per slot.
+template <typename T>
+__device__ __forceinline__ T *slot_ptr(T *base, int64_t per) {
+    return base + blockIdx.y * per;
+}
+
+__device__ __forceinline__ Hot sim_hot(const Hot &h, const SimB &sb) {
+    Hot hh = h;
+    hh.val = sb.val;
+    return hh;
+}
+
+template <bool KD, bool AGG>
+__global__ void __launch_bounds__(PT) k_kds_b(Hot h, const __grid_constant__ BatchTab t,
+                                              float *dens, int64_t M) {
+    const SimB &sb = t.s[blockIdx.y];
+    kds_body<KD, false, false, AGG>(sim_hot(h, sb), sb.pmid, sb.disp, sb.vel, sb.acc, sb.n, sb.f[0],
+                               sb.f[1], slot_ptr(dens, M));
+}
+
+template <bool KICK>
+__global__ void __launch_bounds__(PT) k_gather3_b(Hot h, const __grid_constant__ BatchTab t,
+                                                  int64_t M, const float *g) {
+    const SimB &sb = t.s[blockIdx.y];
+    gather3_body<KICK, false>(sim_hot(h, sb), sb.pmid, sb.disp, sb.vel, sb.acc, sb.n, M,
+                              slot_ptr(g, 3 * M), sb.f[0]);
+}
+
+template <bool AGG>
+__global__ void __launch_bounds__(PT) k_gk_kds_b(Hot h, const __grid_constant__ BatchTab t,
+                                                 int64_t M, const float *g, float *dens) {
+    const SimB &sb = t.s[blockIdx.y];
+    gk_kds_body<AGG>(sim_hot(h, sb), sb.pmid, sb.disp, sb.vel, sb.n, slot_ptr(g, 3 * M), sb.f[0],
+                sb.f[1], sb.f[2], slot_ptr(dens, M));
+}
+
+template <bool KD, bool AGG>
+__global__ void __launch_bounds__(PT) k_ka_b(Hot h, const __grid_constant__ BatchTab t,
+                                             int64_t M, float *dens, double *part) {
+    const SimB &sb = t.s[blockIdx.y];
+    ka_body<KD, false, false, AGG>(sim_hot(h, sb), sb.pmid, sb.disp, sb.vel, sb.acc, sb.dcot, sb.vcot,
+                              sb.alpha, sb.n, sb.f[0], sb.f[1], slot_ptr(dens, M),
+                              slot_ptr(part, (int64_t)NSLOT * PMAX));
+}
+
+// acc_cot: the simulation's vel_cot (steps) or the given cotangent of acc
+// (the force VJP, where it is also vel_cot)
+template <bool AGG>
+__global__ void __launch_bounds__(PT) k_g3adj_b(Hot h, const __grid_constant__ BatchTab t,
+                                                int64_t M, const float *g, float *mcot,
+                                                double *part) {
+    const SimB &sb = t.s[blockIdx.y];
+    g3adj_body<false, AGG>(sim_hot(h, sb), sb.pmid, sb.disp, sb.vcot, sb.acc, sb.alpha, sb.n, M,
+                      slot_ptr(g, 3 * M), slot_ptr(mcot, 3 * M),
+                      slot_ptr(part, (int64_t)NSLOT * PMAX));
+}
+
+template <bool KICK>
+__global__ void __launch_bounds__(PT) k_sadj_b(Hot h, const __grid_constant__ BatchTab t,
+                                               int64_t M, const float *rcot) {
+    const SimB &sb = t.s[blockIdx.y];
+    sadj_body<KICK, false>(sim_hot(h, sb), sb.pmid, sb.disp, sb.vel, sb.acc, sb.dcot, sb.alpha,
+                           sb.n, slot_ptr(rcot, M), sb.f[0]);
+}
+
+template <bool AGG>
+__global__ void __launch_bounds__(PT) k_sa_ka_b(Hot h, const __grid_constant__ BatchTab t,
+                                                int64_t M, const float *rcot, float *dens,
+                                                double *part) {
+    const SimB &sb = t.s[blockIdx.y];
+    sa_ka_body<AGG>(sim_hot(h, sb), sb.pmid, sb.disp, sb.vel, sb.acc, sb.dcot, sb.vcot, sb.alpha, sb.n,
+               slot_ptr(rcot, M), sb.f[0], sb.f[1], sb.f[2], slot_ptr(dens, M),
+               slot_ptr(part, (int64_t)NSLOT * PMAX));
+}
+
+// k_finish of every simulation of a batch (block b: slot b): dots[b][0..3)
+// and the Omega_m term into dots[b][3], or only the latter (ndots 0).
+struct FinishTab {
+    double *dots[BMAX];
+    double oms[BMAX];
+};
+__global__ void k_finish_b(const double *part, int nblk, const __grid_constant__ FinishTab t,
+                           int ndots) {
+    __shared__ double sh[32];
+    const double *pp = part + blockIdx.x * (int64_t)NSLOT * PMAX;
+    double *dots = t.dots[blockIdx.x];
+    for (int s = 0; s < 3; ++s) {
+        if (s >= ndots && s != 2) continue;
+        double v = 0.0;
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += pp[s * PMAX + b];
+        double tt = block_sum<1024>(v, sh);
+        if (threadIdx.x == 0) {
+            if (s < ndots) dots[s] = tt;
+            if (s == 2) dots[3] = t.oms[blockIdx.x] * tt;
         }
     }
 }
@@ -982,6 +1335,7 @@ int device_scratch(double **out) {
             else KERNEL<PMX_UNPAREN KD, true, false><<<grid, PT, wsmem, st>>> args;            \
         } else {                                                                               \
             if ((h).vcomp) KERNEL<PMX_UNPAREN KD, false, true><<<grid, PT, 0, st>>> args;      \
+            else if ((h).agg) KERNEL<PMX_UNPAREN KD, false, false, true><<<grid, PT, 0, st>>> args; \
             else KERNEL<PMX_UNPAREN KD, false, false><<<grid, PT, 0, st>>> args;               \
         }                                                                                      \
     } while (0)
@@ -1015,6 +1369,7 @@ int check_hot(pmx_workspace *ws, const pmx_enmesh_spec *spec, const void *pmid, 
     // measured slower on GB300 (the v4 reductions with two zero lanes cost
     // more than the scalar atomics they replace): opt-in, PMX_WS_VEC
     h->vec = ws->vec;
+    h->agg = ws->agg;
     if (ws->xfast) {
         h->gxs = 2 * ws->n1 * ws->n2;
         h->gjs = ws->n1 * ws->n2;
@@ -1048,10 +1403,11 @@ int poisson_grid(pmx_workspace *ws) {
 // Issues the slab loop of transform `kind` on stream s0: slab i (S x-planes
 // of one component) runs on chain i % nbranch, each chain on its own stream
 // with its own plan, forked from and joined back into s0.
-int slab_issue(pmx_workspace *ws, int kind, const void *in, void *out, cudaStream_t s0) {
+int slab_issue(pmx_workspace *ws, int kind, int nslot, const void *in, void *out,
+               cudaStream_t s0) {
     SlabXf &x = ws->sx[kind];
     const int64_t pr = ws->n1 * ws->n2, pc = ws->n1 * ws->n2h, S = ws->slab;
-    const int64_t np = (kind == 1 || kind == 2) ? 3 * ws->n0 : ws->n0;
+    const int64_t np = nslot * ((kind == 1 || kind == 2) ? 3 * ws->n0 : ws->n0);
     const int K = ws->nbranch;
     if (K > 1) {
         PMX_CUDA(cudaEventRecord(ws->fork, s0));
@@ -1072,19 +1428,21 @@ int slab_issue(pmx_workspace *ws, int kind, const void *in, void *out, cudaStrea
     return PMX_OK;
 }
 
-// Runs transform `kind` (in -> out, all planes) on st: directly, or by
-// launching the CUDA graph of its slab loop, captured on first use (and again
-// if the buffers change).
-int slab_run(pmx_workspace *ws, int kind, const void *in, void *out, cudaStream_t st) {
-    if (!ws->graphs) return slab_issue(ws, kind, in, out, st);
+// Runs transform `kind` (in -> out, all planes of nslot slots) on st:
+// directly, or by launching the CUDA graph of its slab loop, captured on
+// first use for this slot count (and again if the buffers change).
+int slab_run(pmx_workspace *ws, int kind, int nslot, const void *in, void *out,
+             cudaStream_t st) {
+    if (!ws->graphs || nslot > GMAX) return slab_issue(ws, kind, nslot, in, out, st);
     SlabXf &x = ws->sx[kind];
-    if (x.exec && (x.in != in || x.out != out)) {
-        cudaGraphExecDestroy(x.exec);
-        x.exec = nullptr;
+    cudaGraphExec_t &ex = x.exec[nslot];
+    if (ex && (x.in[nslot] != in || x.out[nslot] != out)) {
+        cudaGraphExecDestroy(ex);
+        ex = nullptr;
     }
-    if (!x.exec) {
+    if (!ex) {
         PMX_CUDA(cudaStreamBeginCapture(ws->cap, cudaStreamCaptureModeThreadLocal));
-        int e = slab_issue(ws, kind, in, out, ws->cap);
+        int e = slab_issue(ws, kind, nslot, in, out, ws->cap);
         cudaGraph_t g = nullptr;
         cudaError_t ce = cudaStreamEndCapture(ws->cap, &g);
         if (e) {
@@ -1092,55 +1450,66 @@ int slab_run(pmx_workspace *ws, int kind, const void *in, void *out, cudaStream_
             return e;
         }
         if (ce != cudaSuccess) return cuda_status(ce, "slab graph capture");
-        ce = cudaGraphInstantiate(&x.exec, g, 0);
+        ce = cudaGraphInstantiate(&ex, g, 0);
         cudaGraphDestroy(g);
         if (ce != cudaSuccess) {
-            x.exec = nullptr;
+            ex = nullptr;
             return cuda_status(ce, "slab graph instantiate");
         }
-        x.in = in;
-        x.out = out;
+        x.in[nslot] = in;
+        x.out[nslot] = out;
     }
-    PMX_CUDA(cudaGraphLaunch(x.exec, st));
+    PMX_CUDA(cudaGraphLaunch(ex, st));
     return PMX_OK;
 }
 
-// Forward force up to the three acceleration meshes in ws->g.  With kd, the
-// kick/drift of the forward step (or kick_adj/drift_adj of the reverse step
-// when adj) precede the density deposit.
-int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t st) {
+// Green's function constant of the Poisson solve: -(1.5 Omega_m) / M in
+// the reference's float32 rounding (gravity.py:56-60).
+float green_c(const pmx_workspace *ws, double omega_m) {
     float s = (float)(1.5 * (double)(float)omega_m);
-    float c = (float)((double)s / (double)ws->M);
+    return (float)((double)s / (double)ws->M);
+}
+
+// Forward force up to the three acceleration meshes in ws->g, for the
+// densities of the first nslot slots (slot b: Green's constant c[b]); the
+// slots' spectra and meshes are consecutive, so each plane transform runs
+// over all their planes at once.
+int force_meshes_b(pmx_workspace *ws, int nslot, const float *c, cudaStream_t st) {
     if (ws->xfast) {
         float2 *H = reinterpret_cast<float2 *>(ws->g);  // g is free until the c2r
+        const int64_t pc = ws->n0 * ws->n1 * ws->n2p;  // complex values per slot spectrum
         if (ws->plane) {
             Stage sg(ws, 2, st, 1);
-            int st2 = plane_fft(false, ws->dens, H, ws->ptw, ws->n0, ws->n1, ws->n2, ws->pscr,
-                                ws->pcl, ws->plane16, st);
+            int st2 = plane_fft(false, ws->dens, H, ws->ptw, nslot * ws->n0, ws->n1, ws->n2,
+                                ws->pscr, ws->pcl, ws->plane16, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 2, st, 0);
-            int st2 = slab_run(ws, 0, ws->dens, H, st);
+            int st2 = slab_run(ws, 0, nslot, ws->dens, H, st);
             if (st2) return st2;
         }
         {
-            Stage sg(ws, 3, st, 1);
-            int st2 = xpass(false, H, ws->ck, ws->ktab, ws->tw, ws->n0, ws->n1, ws->n2h, ws->n2p, c,
-                            st);
-            if (st2) return st2;
+            Stage sg(ws, 3, st, nslot);
+            for (int b = 0; b < nslot; ++b) {
+                int st2 = xpass(false, H + b * pc, ws->ck + 3 * b * pc, ws->ktab, ws->tw, ws->n0,
+                                ws->n1, ws->n2h, ws->n2p, c[b], st);
+                if (st2) return st2;
+            }
         }
         if (ws->plane) {
             Stage sg(ws, 4, st, 1);
-            int st2 = plane_fft(true, ws->ck, ws->g, ws->ptw, 3 * ws->n0, ws->n1, ws->n2, ws->pscr,
-                                ws->pcl, ws->plane16, st);
+            int st2 = plane_fft(true, ws->ck, ws->g, ws->ptw, 3 * nslot * ws->n0, ws->n1, ws->n2,
+                                ws->pscr, ws->pcl, ws->plane16, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 4, st, 0);
-            int st2 = slab_run(ws, 1, ws->ck, ws->g, st);
+            int st2 = slab_run(ws, 1, nslot, ws->ck, ws->g, st);
             if (st2) return st2;
         }
         return PMX_OK;
     }
+    if (nslot != 1) return fail(PMX_ERR_SHAPE, "batched calls need the fused x-pass path");
+    const float c0 = c[0];
     {
         Stage sg(ws, 2, st, 0);
         PMX_CUFFT(cufftSetStream(ws->r2c1, st));
@@ -1149,7 +1518,7 @@ int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t s
     {
         Stage sg(ws, 3, st, 1);
         k_poisson_fwd<<<poisson_grid(ws), 256, 0, st>>>(ws->ck, ws->n0, ws->n1, ws->n2h, ws->Mc,
-                                                         ws->ktab, c);
+                                                         ws->ktab, c0);
         PMX_LAUNCH_CHECK("k_poisson_fwd");
     }
     {
@@ -1160,42 +1529,47 @@ int force_meshes(pmx_workspace *ws, const Hot &h, double omega_m, cudaStream_t s
     return PMX_OK;
 }
 
-// The force VJP tail after k_g3adj has filled ws->mcot: r2c of the three
-// cotangent meshes, adjoint Fourier operator, c2r into ws->rcot (then
-// rho_cot, scale folded in).
-int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
-    float s = (float)(1.5 * (double)(float)omega_m);
-    float c = (float)((double)s / (double)ws->M);
+// The force VJP tail after k_g3adj has filled the mesh cotangents of the
+// first nslot slots: r2c of the three cotangent meshes, adjoint Fourier
+// operator, c2r into rcot_of(nslot) (then rho_cot of each slot, scale
+// folded in).
+int force_adj_meshes_b(pmx_workspace *ws, int nslot, const float *c, cudaStream_t st) {
     if (ws->xfast) {
         float2 *Sk = reinterpret_cast<float2 *>(ws->g);  // g is dead after k_g3adj
+        float *rcot = ws->rcot_of(nslot);
+        const int64_t pc = ws->n0 * ws->n1 * ws->n2p;
         if (ws->plane) {
             Stage sg(ws, 8, st, 1);
-            int st2 = plane_fft(false, ws->mcot, ws->ck, ws->ptw, 3 * ws->n0, ws->n1, ws->n2,
-                                ws->pscr, ws->pcl, ws->plane16, st);
+            int st2 = plane_fft(false, ws->mcot, ws->ck, ws->ptw, 3 * nslot * ws->n0, ws->n1,
+                                ws->n2, ws->pscr, ws->pcl, ws->plane16, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 8, st, 0);
-            int st2 = slab_run(ws, 2, ws->mcot, ws->ck, st);
+            int st2 = slab_run(ws, 2, nslot, ws->mcot, ws->ck, st);
             if (st2) return st2;
         }
         {
-            Stage sg(ws, 9, st, 1);
-            int st2 = xpass(true, ws->ck, Sk, ws->ktab, ws->tw, ws->n0, ws->n1, ws->n2h, ws->n2p, c,
-                            st);
-            if (st2) return st2;
+            Stage sg(ws, 9, st, nslot);
+            for (int b = 0; b < nslot; ++b) {
+                int st2 = xpass(true, ws->ck + 3 * b * pc, Sk + b * pc, ws->ktab, ws->tw, ws->n0,
+                                ws->n1, ws->n2h, ws->n2p, c[b], st);
+                if (st2) return st2;
+            }
         }
         if (ws->plane) {
             Stage sg(ws, 10, st, 1);
-            int st2 = plane_fft(true, Sk, ws->rcot, ws->ptw, ws->n0, ws->n1, ws->n2, ws->pscr,
-                                ws->pcl, ws->plane16, st);
+            int st2 = plane_fft(true, Sk, rcot, ws->ptw, nslot * ws->n0, ws->n1, ws->n2,
+                                ws->pscr, ws->pcl, ws->plane16, st);
             if (st2) return st2;
         } else {
             Stage sg(ws, 10, st, 0);
-            int st2 = slab_run(ws, 3, Sk, ws->rcot, st);
+            int st2 = slab_run(ws, 3, nslot, Sk, rcot, st);
             if (st2) return st2;
         }
         return PMX_OK;
     }
+    if (nslot != 1) return fail(PMX_ERR_SHAPE, "batched calls need the fused x-pass path");
+    const float c0 = c[0];
     {
         Stage sg(ws, 8, st, 0);
         PMX_CUFFT(cufftSetStream(ws->r2c3, st));
@@ -1204,15 +1578,25 @@ int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
     {
         Stage sg(ws, 9, st, 1);
         k_poisson_adj<<<poisson_grid(ws), 256, 0, st>>>(ws->ck, ws->n0, ws->n1, ws->n2h, ws->Mc,
-                                                         ws->ktab, c);
+                                                         ws->ktab, c0);
         PMX_LAUNCH_CHECK("k_poisson_adj");
     }
     {
         Stage sg(ws, 10, st, 0);
         PMX_CUFFT(cufftSetStream(ws->c2r1, st));
-        PMX_CUFFT(cufftExecC2R(ws->c2r1, reinterpret_cast<cufftComplex *>(ws->ck), ws->rcot));
+        PMX_CUFFT(cufftExecC2R(ws->c2r1, reinterpret_cast<cufftComplex *>(ws->ck), ws->rcot_of(1)));
     }
     return PMX_OK;
+}
+
+// One simulation (slot 0) of the workspace.
+int force_meshes(pmx_workspace *ws, const Hot &, double omega_m, cudaStream_t st) {
+    const float c = green_c(ws, omega_m);
+    return force_meshes_b(ws, 1, &c, st);
+}
+int force_adj_meshes(pmx_workspace *ws, double omega_m, cudaStream_t st) {
+    const float c = green_c(ws, omega_m);
+    return force_adj_meshes_b(ws, 1, &c, st);
 }
 
 double om_scale(double omega_m) {
@@ -1267,7 +1651,8 @@ void ws_free(pmx_workspace *ws) {
     if (ws->have_r2c3) cufftDestroy(ws->r2c3);
     if (ws->have_c2r1) cufftDestroy(ws->c2r1);
     for (auto &x : ws->sx) {
-        if (x.exec) cudaGraphExecDestroy(x.exec);
+        for (auto e : x.exec)
+            if (e) cudaGraphExecDestroy(e);
         for (int k = 0; k < KMAX; ++k) {
             if (x.have[k]) cufftDestroy(x.plan[k]);
             cudaFree(x.work[k]);
@@ -1297,12 +1682,12 @@ void ws_free(pmx_workspace *ws) {
     delete ws;
 }
 
-size_t buffers_bytes(const int64_t s[3], int32_t flags) {
+size_t buffers_bytes(const int64_t s[3], int32_t flags, int32_t slots) {
     int64_t M = s[0] * s[1] * s[2], Mc = s[0] * s[1] * (s[2] / 2 + 1);
     size_t b = (size_t)M * 4 + (size_t)Mc * 8 * 3 + (size_t)M * 4 * 3;
     if (flags & PMX_WS_ADJOINT) b += (size_t)M * 4 * 3;
-    b += (size_t)2 * (s[0] + s[1] + s[2] / 2 + 1) * 4 + (size_t)NSLOT * PMAX * 8;
-    return b;
+    b += (size_t)NSLOT * PMAX * 8;
+    return b * (size_t)slots + (size_t)2 * (s[0] + s[1] + s[2] / 2 + 1) * 4;
 }
 
 int check_shape(const int64_t s[3]) {
@@ -1317,7 +1702,7 @@ extern "C" int pmx_workspace_bytes(const int64_t mesh_shape[3], int32_t flags, s
     if (!mesh_shape || !bytes) return fail(PMX_ERR_ARG, "null argument");
     int st = check_shape(mesh_shape);
     if (st) return st;
-    size_t total = buffers_bytes(mesh_shape, flags), wmax = 0;
+    size_t total = buffers_bytes(mesh_shape, flags, 1), wmax = 0;
     cufftType types[4] = {CUFFT_R2C, CUFFT_C2R, CUFFT_R2C, CUFFT_C2R};
     int64_t batches[4] = {1, 3, 3, 1};
     int nplans = (flags & PMX_WS_ADJOINT) ? 4 : 2;
@@ -1332,13 +1717,15 @@ extern "C" int pmx_workspace_bytes(const int64_t mesh_shape[3], int32_t flags, s
     return PMX_OK;
 }
 
-extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
-                                    pmx_workspace **out) {
+static int ws_create(const int64_t mesh_shape[3], int32_t flags, int32_t slots,
+                     pmx_workspace **out) {
     if (!mesh_shape || !out) return fail(PMX_ERR_ARG, "null argument");
     int st = check_shape(mesh_shape);
     if (st) return st;
+    if (slots < 1 || slots > BMAX) return fail(PMX_ERR_ARG, "slots must be in 1..16");
     pmx_workspace *ws = new pmx_workspace();
     ws->flags = flags;
+    ws->slots = slots;
     ws->n0 = mesh_shape[0];
     ws->n1 = mesh_shape[1];
     ws->n2 = mesh_shape[2];
@@ -1361,18 +1748,18 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
     ws->plane = ws->xfast && plane_supported(ws->n1, ws->n2) && (flags & PMX_WS_PLANE);
     ws->plane16 = (flags & PMX_WS_PLANE16) != 0;
     ws->vec = ws->n2 % 4 == 0 && (flags & PMX_WS_VEC);
+    ws->agg = (flags & PMX_WS_AGG) && (uint64_t)ws->M * (uint64_t)slots < 0xFFFFFFE0ull;
     ws->n2p = ws->plane ? padded_row(ws->n2h) : ws->n2h;
     int64_t ktn = 2 * (ws->n0 + ws->n1 + ws->n2h);
-    if ((st = alloc((void **)&ws->dens, ws->M * 4)) ||
-        (st = alloc((void **)&ws->ck, ws->n0 * ws->n1 * ws->n2p * 8 * 3)) ||
-        (st = alloc((void **)&ws->g, ws->M * 4 * 3)) || (st = alloc((void **)&ws->ktab, ktn * 4)) ||
-        (st = alloc((void **)&ws->part, NSLOT * PMAX * 8)) ||
-        ((flags & PMX_WS_ADJOINT) && (st = alloc((void **)&ws->mcot, ws->M * 4 * 3)))) {
+    const int64_t B = slots;
+    if ((st = alloc((void **)&ws->dens, B * ws->M * 4)) ||
+        (st = alloc((void **)&ws->ck, B * ws->n0 * ws->n1 * ws->n2p * 8 * 3)) ||
+        (st = alloc((void **)&ws->g, B * ws->M * 4 * 3)) || (st = alloc((void **)&ws->ktab, ktn * 4)) ||
+        (st = alloc((void **)&ws->part, B * NSLOT * PMAX * 8)) ||
+        ((flags & PMX_WS_ADJOINT) && (st = alloc((void **)&ws->mcot, B * ws->M * 4 * 3)))) {
         ws_free(ws);
         return st;
     }
-    // rcot behind the complex spectrum held in g (2 n0 n1 n2p + M <= 3 M floats)
-    ws->rcot = ws->g + 2 * ws->n0 * ws->n1 * ws->n2p;
     ws->win = (ws->n2 % 4 == 0) && (flags & PMX_WS_WINDOW);
     if (ws->win) {
         cudaError_t e = cudaFuncSetAttribute(k_g3adj<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1481,6 +1868,16 @@ extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
     return PMX_OK;
 }
 
+extern "C" int pmx_workspace_create(const int64_t mesh_shape[3], int32_t flags,
+                                    pmx_workspace **out) {
+    return ws_create(mesh_shape, flags, 1, out);
+}
+
+extern "C" int pmx_workspace_create_batch(const int64_t mesh_shape[3], int32_t flags,
+                                          int32_t slots, pmx_workspace **out) {
+    return ws_create(mesh_shape, flags, slots, out);
+}
+
 extern "C" int pmx_workspace_destroy(pmx_workspace *ws) {
     if (!ws) return PMX_OK;
     cudaDeviceSynchronize();
@@ -1558,6 +1955,9 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
             if (h.win)
                 k_g3adj<true><<<G, PT, WIN3_SMEM, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M,
                                                        ws->g, ws->mcot, ws->part);
+            else if (h.agg)
+                k_g3adj<false, true><<<G, PT, 0, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M,
+                                                      ws->g, ws->mcot, ws->part);
             else
                 k_g3adj<false><<<G, PT, 0, s>>>(h, pmid, disp, acc_cot, acc, disp_cot, n, ws->M, ws->g,
                                                 ws->mcot, ws->part);
@@ -1569,7 +1969,7 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
         {
             Stage sg(ws, 11, s, 1);
             k_sadj<false, false><<<G, PT, 0, s>>>(h, pmid, disp, nullptr, nullptr, nullptr, disp_cot,
-                                                  n, ws->rcot, 0.f);
+                                                  n, ws->rcot_of(1), 0.f);
             PMX_LAUNCH_CHECK("k_sadj");
         }
     }
@@ -1760,6 +2160,9 @@ static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const 
         if (h.win)
             k_g3adj<true><<<G, PT, WIN3_SMEM, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M,
                                                    ws->g, ws->mcot, ws->part);
+        else if (h.agg)
+            k_g3adj<false, true><<<G, PT, 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M,
+                                                  ws->g, ws->mcot, ws->part);
         else
             k_g3adj<false><<<G, PT, 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M, ws->g,
                                             ws->mcot, ws->part);
@@ -1770,10 +2173,10 @@ static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const 
         Stage sg(ws, 11, s, 1);
         if (h.vcomp)
             k_sadj<true, true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n,
-                                                ws->rcot, factors[2]);
+                                                ws->rcot_of(1), factors[2]);
         else
             k_sadj<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n,
-                                                 ws->rcot, factors[2]);
+                                                 ws->rcot_of(1), factors[2]);
         PMX_LAUNCH_CHECK("k_sadj");
     }
     {
@@ -1854,8 +2257,12 @@ static int nbody_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int
     }
     {
         Stage sg(ws, 1, s, 1);
-        k_kds<true, false, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, factors[0],
-                                                     factors[1], ws->dens);
+        if (h.agg)
+            k_kds<true, false, false, true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, factors[0],
+                                                             factors[1], ws->dens);
+        else
+            k_kds<true, false, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, factors[0],
+                                                         factors[1], ws->dens);
         PMX_LAUNCH_CHECK("k_kds");
     }
     for (int32_t i = 0; i < nsteps; ++i) {
@@ -1868,7 +2275,11 @@ static int nbody_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int
                 PMX_LAUNCH_CHECK("k_fill");
             }
             Stage sg(ws, 13, s, 1);
-            k_gk_kds<<<G, PT, 0, s>>>(h, pmid, disp, vel, n, ws->g, f[2], f[3], f[4], ws->dens);
+            if (h.agg)
+                k_gk_kds<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, n, ws->g, f[2], f[3], f[4],
+                                                ws->dens);
+            else
+                k_gk_kds<<<G, PT, 0, s>>>(h, pmid, disp, vel, n, ws->g, f[2], f[3], f[4], ws->dens);
             PMX_LAUNCH_CHECK("k_gk_kds");
         } else {
             Stage sg(ws, 5, s, 1);
@@ -1912,9 +2323,14 @@ static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const
     }
     {
         Stage sg(ws, 6, s, 1);
-        k_ka<true, false, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot,
-                                                    acc_cot, n, factors[0], factors[1], ws->dens,
-                                                    ws->part);
+        if (h.agg)
+            k_ka<true, false, false, true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot,
+                                                            vel_cot, acc_cot, n, factors[0],
+                                                            factors[1], ws->dens, ws->part);
+        else
+            k_ka<true, false, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot,
+                                                        acc_cot, n, factors[0], factors[1],
+                                                        ws->dens, ws->part);
         PMX_LAUNCH_CHECK("k_ka");
     }
     for (int32_t i = 0; i < nsteps; ++i) {
@@ -1922,8 +2338,12 @@ static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const
         if ((st = force_meshes(ws, h, omega_m, s))) return st;
         {
             Stage sg(ws, 7, s, 1);
-            k_g3adj<false><<<G, PT, 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M, ws->g,
-                                            ws->mcot, ws->part);
+            if (h.agg)
+                k_g3adj<false, true><<<G, PT, 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M,
+                                                      ws->g, ws->mcot, ws->part);
+            else
+                k_g3adj<false><<<G, PT, 0, s>>>(h, pmid, disp, vel_cot, acc, acc_cot, n, ws->M,
+                                                ws->g, ws->mcot, ws->part);
             PMX_LAUNCH_CHECK("k_g3adj");
         }
         {
@@ -1941,13 +2361,18 @@ static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const
                 PMX_LAUNCH_CHECK("k_fill");
             }
             Stage sg(ws, 14, s, 1);
-            k_sa_ka<<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n,
-                                     ws->rcot, f[2], f[3], f[4], ws->dens, ws->part);
+            if (h.agg)
+                k_sa_ka<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot,
+                                               n, ws->rcot_of(1), f[2], f[3], f[4], ws->dens,
+                                               ws->part);
+            else
+                k_sa_ka<<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n,
+                                         ws->rcot_of(1), f[2], f[3], f[4], ws->dens, ws->part);
             PMX_LAUNCH_CHECK("k_sa_ka");
         } else {
             Stage sg(ws, 11, s, 1);
             k_sadj<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n,
-                                                 ws->rcot, f[2]);
+                                                 ws->rcot_of(1), f[2]);
             PMX_LAUNCH_CHECK("k_sadj");
         }
     }
@@ -1969,6 +2394,230 @@ extern "C" int pmx_nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spe
                                    double omega_m, double *dots, void *stream) {
     return nbody_adj_steps(ws, spec, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n,
                            ptcl_num, nsteps, factors, omega_m, dots, stream);
+}
+
+// ---------------------------------------------------------------------------
+// batched simulations (equal mesh shape and cell size, one slot each)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct BatchCall {
+    Hot h;
+    BatchTab tab;
+    float c[BMAX];       // Green's constant per simulation
+    FinishTab fin;
+    int nb = 0;
+    int G = 1;           // blocks per simulation
+};
+
+// Every host-side check of a batched call, before anything is launched.
+int batch_prepare(pmx_workspace *ws, const pmx_enmesh_spec *spec, int32_t nsim,
+                  const pmx_sim *sims, bool adjoint, int32_t nsteps, BatchCall *bc) {
+    if (nsteps < 0) return fail(PMX_ERR_ARG, "negative nsteps");
+    if (!ws) return fail(PMX_ERR_ARG, "null workspace");
+    if (!sims || nsim < 1) return fail(PMX_ERR_ARG, "no simulations");
+    if (nsim > ws->slots || nsim > BMAX)
+        return fail(PMX_ERR_ARG, "more simulations than the workspace's slots");
+    if (!ws->xfast) return fail(PMX_ERR_SHAPE, "batched calls need the fused x-pass path");
+    if (ws->win) return fail(PMX_ERR_ARG, "batched calls use the plain deposits (no windows)");
+    if (adjoint && !(ws->flags & PMX_WS_ADJOINT))
+        return fail(PMX_ERR_ARG, "workspace lacks PMX_WS_ADJOINT");
+    int st = check_hot(ws, spec, sims[0].pmid, sims[0].disp, sims[0].n, sims[0].ptcl_num, &bc->h);
+    if (st) return st;
+    bc->nb = nsim;
+    int64_t nmax = 0;
+    for (int b = 0; b < nsim; ++b) {
+        const pmx_sim &q = sims[b];
+        if (q.n < 0 || q.ptcl_num <= 0) return fail(PMX_ERR_ARG, "bad particle counts");
+        if (q.n > 0 && (!q.pmid || !q.disp || !q.vel || !q.acc))
+            return fail(PMX_ERR_ARG, "null particle array");
+        if (adjoint && q.n > 0 && (!q.disp_cot || !q.vel_cot || !q.acc_cot))
+            return fail(PMX_ERR_ARG, "null cotangent array");
+        if (adjoint && !q.dots) return fail(PMX_ERR_ARG, "null dots");
+        if (nsteps > 0 && !q.factors) return fail(PMX_ERR_ARG, "null factors");
+        SimB &sb = bc->tab.s[b];
+        sb.pmid = q.pmid;
+        sb.disp = q.disp;
+        sb.vel = q.vel;
+        sb.acc = q.acc;
+        sb.dcot = q.disp_cot;
+        sb.vcot = q.vel_cot;
+        sb.alpha = q.acc_cot;
+        sb.n = q.n;
+        sb.val = (float)((double)ws->M / (double)q.ptcl_num);
+        bc->c[b] = green_c(ws, q.omega_m);
+        bc->fin.dots[b] = q.dots;
+        bc->fin.oms[b] = om_scale(q.omega_m);
+        if (q.n > nmax) nmax = q.n;
+    }
+    int G = stride_grid(nmax, PT);
+    bc->G = G > PMAX ? PMAX : G;
+    return PMX_OK;
+}
+
+// Sets every simulation's launch factors f[0..2] from its factor table:
+// f[j] = factors[3 i + off + j] for j < cnt (else 0).
+int batch_factors(BatchCall *bc, const pmx_sim *sims, int i, int off, int cnt) {
+    for (int b = 0; b < bc->nb; ++b) {
+        for (int j = 0; j < 3; ++j)
+            bc->tab.s[b].f[j] = j < cnt ? sims[b].factors[3 * i + off + j] : 0.f;
+    }
+    return PMX_OK;
+}
+
+}  // namespace
+
+extern "C" int pmx_nbody_steps_batch(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                                     int32_t nsim, const pmx_sim *sims, int32_t init_force,
+                                     int32_t nsteps, void *stream) {
+    BatchCall bc;
+    int st = batch_prepare(ws, spec, nsim, sims, false, nsteps, &bc);
+    if (st) return st;
+    if (!init_force && nsteps == 0) return PMX_OK;
+    cudaStream_t s = as_stream(stream);
+    if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
+    const int64_t M = ws->M, nb = bc.nb;
+    const dim3 grid(bc.G, bc.nb);
+    auto fill_dens = [&]() -> int {
+        Stage sg(ws, 0, s, 1);
+        k_fill<<<grid_fill(nb * M), 256, 0, s>>>(ws->dens, -1.f, nb * M);
+        PMX_LAUNCH_CHECK("k_fill");
+        return PMX_OK;
+    };
+    if ((st = fill_dens())) return st;
+    if (init_force) {   // acc = F(disp), as pmx_force
+        {
+            Stage sg(ws, 1, s, 1);
+            if (bc.h.agg) k_kds_b<false, true><<<grid, PT, 0, s>>>(bc.h, bc.tab, ws->dens, M);
+            else k_kds_b<false, false><<<grid, PT, 0, s>>>(bc.h, bc.tab, ws->dens, M);
+            PMX_LAUNCH_CHECK("k_kds_b");
+        }
+        if ((st = force_meshes_b(ws, bc.nb, bc.c, s))) return st;
+        {
+            Stage sg(ws, 5, s, 1);
+            k_gather3_b<false><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, ws->g);
+            PMX_LAUNCH_CHECK("k_gather3_b");
+        }
+        if (nsteps == 0) return PMX_OK;
+        if ((st = fill_dens())) return st;
+    }
+    if ((st = batch_factors(&bc, sims, 0, 0, 2))) return st;
+    {
+        Stage sg(ws, 1, s, 1);
+        if (bc.h.agg) k_kds_b<true, true><<<grid, PT, 0, s>>>(bc.h, bc.tab, ws->dens, M);
+        else k_kds_b<true, false><<<grid, PT, 0, s>>>(bc.h, bc.tab, ws->dens, M);
+        PMX_LAUNCH_CHECK("k_kds_b");
+    }
+    for (int32_t i = 0; i < nsteps; ++i) {
+        if ((st = force_meshes_b(ws, bc.nb, bc.c, s))) return st;
+        if (i + 1 < nsteps) {
+            if ((st = fill_dens())) return st;
+            if ((st = batch_factors(&bc, sims, i, 2, 3))) return st;   // K2_i, K1_i+1, D_i+1
+            Stage sg(ws, 13, s, 1);
+            if (bc.h.agg) k_gk_kds_b<true><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, ws->g, ws->dens);
+            else k_gk_kds_b<false><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, ws->g, ws->dens);
+            PMX_LAUNCH_CHECK("k_gk_kds_b");
+        } else {
+            if ((st = batch_factors(&bc, sims, i, 2, 1))) return st;   // K2_i
+            Stage sg(ws, 5, s, 1);
+            k_gather3_b<true><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, ws->g);
+            PMX_LAUNCH_CHECK("k_gather3_b");
+        }
+    }
+    return PMX_OK;
+}
+
+extern "C" int pmx_nbody_adj_steps_batch(pmx_workspace *ws, const pmx_enmesh_spec *spec,
+                                         int32_t nsim, const pmx_sim *sims, int32_t init_vjp,
+                                         int32_t nsteps, void *stream) {
+    BatchCall bc;
+    int st = batch_prepare(ws, spec, nsim, sims, true, nsteps, &bc);
+    if (st) return st;
+    if (!init_vjp && nsteps == 0) return PMX_OK;
+    cudaStream_t s = as_stream(stream);
+    if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
+    const int64_t M = ws->M, nb = bc.nb;
+    const dim3 grid(bc.G, bc.nb);
+    float *rcot = ws->rcot_of(bc.nb);
+    auto fills = [&]() -> int {
+        Stage sg(ws, 0, s, 2);
+        k_fill<<<grid_fill(nb * M), 256, 0, s>>>(ws->dens, -1.f, nb * M);
+        k_fill<<<grid_fill(3 * nb * M), 256, 0, s>>>(ws->mcot, 0.f, 3 * nb * M);
+        PMX_LAUNCH_CHECK("k_fill");
+        return PMX_OK;
+    };
+    auto finish = [&](int64_t row, int ndots) -> int {
+        FinishTab ft = bc.fin;
+        for (int b = 0; b < bc.nb; ++b) ft.dots[b] = bc.fin.dots[b] + 4 * row;
+        Stage sg(ws, 12, s, 1);
+        k_finish_b<<<bc.nb, 1024, 0, s>>>(ws->part, bc.G, ft, ndots);
+        PMX_LAUNCH_CHECK("k_finish_b");
+        return PMX_OK;
+    };
+    if (init_vjp) {   // the force VJP of acc_cot = vel_cot, as pmx_force_vjp
+        if ((st = fills())) return st;
+        {
+            Stage sg(ws, 1, s, 1);
+            if (bc.h.agg) k_kds_b<false, true><<<grid, PT, 0, s>>>(bc.h, bc.tab, ws->dens, M);
+            else k_kds_b<false, false><<<grid, PT, 0, s>>>(bc.h, bc.tab, ws->dens, M);
+            PMX_LAUNCH_CHECK("k_kds_b");
+        }
+        if ((st = force_meshes_b(ws, bc.nb, bc.c, s))) return st;
+        {
+            Stage sg(ws, 7, s, 1);
+            if (bc.h.agg) k_g3adj_b<true><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, ws->g, ws->mcot, ws->part);
+            else k_g3adj_b<false><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, ws->g, ws->mcot, ws->part);
+            PMX_LAUNCH_CHECK("k_g3adj_b");
+        }
+        if ((st = force_adj_meshes_b(ws, bc.nb, bc.c, s))) return st;
+        {
+            Stage sg(ws, 11, s, 1);
+            k_sadj_b<false><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, rcot);
+            PMX_LAUNCH_CHECK("k_sadj_b");
+        }
+        if ((st = finish(nsteps, 0))) return st;
+        if (nsteps == 0) return PMX_OK;
+    }
+    if ((st = fills())) return st;
+    if ((st = batch_factors(&bc, sims, 0, 0, 2))) return st;
+    {
+        Stage sg(ws, 6, s, 1);
+        if (bc.h.agg) k_ka_b<true, true><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, ws->dens, ws->part);
+        else k_ka_b<true, false><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, ws->dens, ws->part);
+        PMX_LAUNCH_CHECK("k_ka_b");
+    }
+    for (int32_t i = 0; i < nsteps; ++i) {
+        if ((st = force_meshes_b(ws, bc.nb, bc.c, s))) return st;
+        {
+            Stage sg(ws, 7, s, 1);
+            if (bc.h.agg) k_g3adj_b<true><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, ws->g, ws->mcot, ws->part);
+            else k_g3adj_b<false><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, ws->g, ws->mcot, ws->part);
+            PMX_LAUNCH_CHECK("k_g3adj_b");
+        }
+        if ((st = finish(i, 3))) return st;
+        if ((st = force_adj_meshes_b(ws, bc.nb, bc.c, s))) return st;
+        if (i + 1 < nsteps) {
+            if ((st = fills())) return st;
+            if ((st = batch_factors(&bc, sims, i, 2, 3))) return st;
+            Stage sg(ws, 14, s, 1);
+            if (bc.h.agg) k_sa_ka_b<true><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, rcot, ws->dens, ws->part);
+            else k_sa_ka_b<false><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, rcot, ws->dens, ws->part);
+            PMX_LAUNCH_CHECK("k_sa_ka_b");
+        } else {
+            if ((st = batch_factors(&bc, sims, i, 2, 1))) return st;
+            Stage sg(ws, 11, s, 1);
+            k_sadj_b<true><<<grid, PT, 0, s>>>(bc.h, bc.tab, M, rcot);
+            PMX_LAUNCH_CHECK("k_sadj_b");
+        }
+    }
+    return PMX_OK;
+}
+
+extern "C" int pmx_workspace_slots(const pmx_workspace *ws, int32_t *slots) {
+    if (!ws || !slots) return fail(PMX_ERR_ARG, "null argument");
+    *slots = ws->slots;
+    return PMX_OK;
 }
 
 extern "C" int pmx_profile_enable(pmx_workspace *ws, int on) {

@@ -3,25 +3,33 @@
 Requests differ in particle grid, mesh factor, step count, cosmology and
 white-noise seed; some ask for the gradient of the squared-density
 objective (forward run, then pmwd's reversible adjoint, nbody.py:251-276).
-The server
+pmwd itself runs one simulation per host loop (nbody.py:216-223); the
+server
 
 * admits requests as they arrive while their device memory fits an HBM
-  budget (particle state + cotangents + a mesh workspace; workspaces are
-  pooled and reused per mesh shape);
+  budget (particle state and cotangents per request, plus the batched
+  workspaces of the mesh groups in use); a request larger than the whole
+  budget is rejected at once with an error result;
 * prepares each admitted request (float64 background tables, white noise,
   2LPT) on a host worker thread, so host work overlaps device work;
-* runs every simulation as a job on its own CUDA stream and advances the
-  jobs in turn a few leapfrog steps (forward or adjoint; one multi-step call
-  of up to STEP_CHUNK steps) at a time, so kernels of different simulations
-  overlap on the device and a newly admitted request starts while others
-  are mid-run (continuous batching at step granularity);
-* retires a job when the event after its last work completes, frees its
-  slot and memory, and admits waiting requests;
+* groups the admitted simulations that share a mesh shape and cell size
+  and are in the same phase (forward or adjoint steps): each group
+  advances a chunk of leapfrog steps in ONE batched call
+  (pmx_nbody_steps_batch / pmx_nbody_adj_steps_batch), whose particle
+  kernels serve every simulation of the group in one launch and whose plane
+  transforms run over all their meshes at once; meshes the fused x pass
+  does not cover run one simulation per call;
+* lets newly admitted requests join their group at the next chunk while the
+  others are mid-run (continuous batching at step granularity);
+* isolates failures: a request whose host setup or device call raises, or
+  that is cancelled, ends with an error result, its slot and memory are
+  freed once nothing of it is in flight, and every other request goes on;
 * records per-request latency (arrival -> result ready): sims/s, p50, p99.
 
-Each job runs exactly the kernels a stand-alone run would (own workspace,
-own stream), so a result is the same alone and in the mix up to the order
-of float32 atomic adds.
+The scheduling logic (``Scheduler``) is host code over an engine interface;
+``GpuEngine`` issues the device work.  A simulation's arithmetic is the one
+of the single-simulation path, so a result is the same alone and in the mix
+up to the order of float32 atomic adds.
 """
 
 import ctypes
@@ -45,9 +53,11 @@ from .scatter import scatter
 
 _nb = importlib.import_module('pmwd_gb300.nbody')
 
-# leapfrog steps a job issues per scheduling turn (one multi-step call, in
+# leapfrog steps a group issues per scheduling turn (one batched call, in
 # which consecutive steps share particle passes)
 STEP_CHUNK = 8
+# most simulations per batched call
+MAX_SLOTS = 8
 
 
 @dataclass
@@ -68,15 +78,16 @@ class Request:
 class Result:
     rid: int
     latency: float
-    disp_rms: float                  # rms displacement at a = 1
-    obj: float                       # sum of squared density contrast at a = 1
+    disp_rms: float = None           # rms displacement at a = 1
+    obj: float = None                # sum of squared density contrast at a = 1
     grad_rms: float = None           # rms of d obj / d (real white-noise modes)
     dobj_dOm: float = None           # d obj / d Omega_m
+    error: str = None                # why the request failed (None: it did not)
     state: dict = field(default=None, repr=False)
 
 
 def request_bytes(side, grad):
-    """Device bytes of a request besides its workspace: particle state
+    """Device bytes of a request besides the workspaces: particle state
     (42 B per particle), cotangents and Kahan-free adjoint state (36 B), and
     the initial-condition transients (~64 B per particle at peak)."""
     n = side ** 3
@@ -84,61 +95,343 @@ def request_bytes(side, grad):
 
 
 def workspace_bytes(mesh_side):
-    """Meshes and spectra of a workspace plus a cuFFT work-area allowance."""
+    """Meshes and spectra of one workspace slot plus a cuFFT work-area
+    allowance."""
     m = mesh_side ** 3
     mc = mesh_side * mesh_side * (mesh_side // 2 + 1)
     return 4 * m + 3 * 8 * mc + 6 * 4 * m + 8 * mc
 
 
-class WorkspacePool:
-    """Reusable workspaces per (device, mesh shape); one job at a time uses
-    a workspace (its buffers and cuFFT plans are bound to the job's
-    stream)."""
+def batchable(mesh_side):
+    """Meshes of the fused x-pass path, which batched calls need."""
+    return mesh_side in (64, 128, 256, 512, 1024)
 
-    def __init__(self):
-        self.free = {}
+
+def group_slots(mesh_side, budget):
+    """Simulations per batched workspace: up to MAX_SLOTS, with the
+    workspace at most a quarter of the budget; 1 where batching does not
+    apply."""
+    if not batchable(mesh_side):
+        return 1
+    return int(max(1, min(MAX_SLOTS, (0.25 * budget) // workspace_bytes(mesh_side))))
+
+
+class Job:
+    """Host-side state of one admitted request.  Phases: setup -> fwd ->
+    objective -> (adj_init -> adj -> backprop) -> done; or failed."""
+
+    def __init__(self, req, t_arr, cost):
+        self.req = req
+        self.t_arr = t_arr
+        self.cost = cost
+        self.key = (req.ptcl_side * req.mesh_factor,
+                    req.ptcl_spacing / req.mesh_factor)   # mesh side, cell size
+        self.phase = 'setup'
+        self.i = 0                  # steps done in the current phase
+        self.init = True            # forward: the first call also computes acc
+        self.cancel = False
+        self.error = None
+        self.future = None
+        self.dev = None             # engine state
+
+
+class Scheduler:
+    """Admission, grouping, chunked stepping, failure isolation and
+    cancellation over an engine (``GpuEngine`` or a test double):
+
+    * engine.slots(key) -> simulations per call for a group key;
+    * engine.group_bytes(key) -> device bytes of that group's shared
+      workspace; engine.job_bytes(req) -> device bytes of one request;
+    * engine.setup(job) (worker thread; may raise);
+    * engine.fwd(jobs, init, k) / engine.adj_init(jobs) / engine.adj(jobs, k):
+      one call for jobs of one key, in the same phase (may raise);
+    * engine.objective(job) / engine.backprop(job) (may raise);
+    * engine.idle(job) -> nothing of the job is in flight on the device;
+    * engine.result(job) -> Result; engine.release(job); engine.drop(key).
+    """
+
+    def __init__(self, engine, budget_bytes=150e9, max_jobs=64, host_workers=4):
+        self.engine = engine
+        self.budget = budget_bytes
+        self.max_jobs = max_jobs
+        self.host_workers = host_workers
+        self._cancel = set()
+        self._lock = threading.Lock()
+
+    def cost(self, req):
+        return self.engine.job_bytes(req)
+
+    def cancel(self, rid):
+        """Cancels request ``rid`` (thread-safe): a waiting request is dropped,
+        an active one stops at its next step boundary; its result carries
+        error 'cancelled'."""
+        with self._lock:
+            self._cancel.add(rid)
+
+    def run(self, requests, realtime=True, on_turn=None):
+        """Serve ``requests`` (arrival offsets in seconds; realtime=False
+        makes all available at t = 0).  Returns (results in request order,
+        stats).  ``on_turn(scheduler, t)`` is called once per scheduling turn
+        (tests use it to cancel)."""
+        eng = self.engine
+        pending = sorted(requests, key=lambda r: r.arrival)
+        qi = 0
+        waiting, active = [], []
+        used = 0.0
+        groups = {}                 # key -> bytes charged for its workspace
+        results = {}
+        ex = ThreadPoolExecutor(max_workers=self.host_workers)
+        t0 = time.perf_counter()
+
+        def now():
+            return time.perf_counter() - t0
+
+        def finish(job, res):
+            res.latency = now() - job.t_arr
+            results[job.req.rid] = res
+
+        def fail(job, err):
+            job.error = err
+            job.phase = 'failed'
+
+        try:
+            while qi < len(pending) or waiting or active:
+                t = now()
+                if on_turn is not None:
+                    on_turn(self, t)
+                while qi < len(pending) and (not realtime or pending[qi].arrival <= t):
+                    waiting.append(pending[qi])
+                    qi += 1
+                with self._lock:
+                    cancels = set(self._cancel)
+                for r in [r for r in waiting if r.rid in cancels]:
+                    waiting.remove(r)
+                    results[r.rid] = Result(r.rid, 0.0, error='cancelled')
+                for job in active:
+                    if job.req.rid in cancels and job.phase not in ('done', 'failed'):
+                        job.cancel = True
+                # admission by HBM budget (request state + new group workspaces)
+                while waiting and len(active) < self.max_jobs:
+                    req = waiting[0]
+                    key = (req.ptcl_side * req.mesh_factor, req.ptcl_spacing / req.mesh_factor)
+                    c = self.cost(req)
+                    g = 0.0 if key in groups else eng.group_bytes(key)
+                    if c + eng.group_bytes(key) > self.budget:
+                        waiting.pop(0)
+                        results[req.rid] = Result(req.rid, 0.0, error=(
+                            f'over budget: needs {(c + eng.group_bytes(key)) / 1e9:.2f} GB of '
+                            f'{self.budget / 1e9:.2f} GB'))
+                        continue
+                    if used + c + g > self.budget:
+                        # free the workspaces of groups nobody uses any more
+                        live = {j.key for j in active}
+                        for k in [k for k in groups if k not in live]:
+                            used -= groups.pop(k)
+                            eng.drop(k)
+                        g = 0.0 if key in groups else eng.group_bytes(key)
+                        if used + c + g > self.budget:
+                            break
+                    waiting.pop(0)
+                    if key not in groups:
+                        groups[key] = eng.group_bytes(key)
+                        used += groups[key]
+                    job = Job(req, req.arrival if realtime else 0.0, c)
+                    job.future = ex.submit(eng.setup, job)
+                    used += c
+                    active.append(job)
+                if not active:
+                    if qi < len(pending):
+                        time.sleep(max(0.0, min(0.002, pending[qi].arrival - now())))
+                    continue
+                moved = False
+                # per-job phases
+                for job in active:
+                    try:
+                        if job.cancel and job.phase not in ('failed', 'done'):
+                            fail(job, 'cancelled')
+                        if job.phase == 'setup' and job.future.done():
+                            job.future.result()          # re-raises the setup error
+                            job.phase = 'fwd'
+                            moved = True
+                        elif job.phase == 'objective':
+                            eng.objective(job)
+                            job.phase = 'adj_init' if job.req.grad else 'done'
+                            moved = True
+                        elif job.phase == 'backprop' and eng.idle(job):
+                            eng.backprop(job)
+                            job.phase = 'done'
+                            moved = True
+                    except Exception as e:               # isolate this request
+                        fail(job, f'{type(e).__name__}: {e}')
+                        moved = True
+                # grouped device phases: one call per (key, phase) group
+                moved |= self._step_groups(active, fail)
+                # retire finished and failed jobs once nothing of them is in flight
+                for job in list(active):
+                    if job.phase not in ('done', 'failed') or not job.future.done():
+                        continue                         # running, or its setup still is
+                    if eng.idle(job):
+                        if job.phase == 'done':
+                            try:
+                                res = eng.result(job)
+                            except Exception as e:
+                                res = Result(job.req.rid, 0.0, error=f'{type(e).__name__}: {e}')
+                        else:
+                            res = Result(job.req.rid, 0.0, error=job.error)
+                        finish(job, res)
+                        eng.release(job)
+                        used -= job.cost
+                        active.remove(job)
+                        moved = True
+                if not moved:
+                    # every job waits on host setup or the device: yield the
+                    # GIL to the setup threads instead of spinning
+                    time.sleep(2e-4)
+        finally:
+            ex.shutdown(wait=True)
+            for k in list(groups):
+                eng.drop(k)
+        eng.synchronize()
+        wall = now()
+        ok = [r for r in results.values() if r.error is None]
+        lat = np.array([r.latency for r in ok])
+        stats = {'sims': len(ok), 'failed': len(results) - len(ok), 'wall_s': wall,
+                 'sims_per_s': len(ok) / wall,
+                 'p50_s': float(np.percentile(lat, 50)) if len(lat) else None,
+                 'p99_s': float(np.percentile(lat, 99)) if len(lat) else None}
+        return [results[r.rid] for r in requests], stats
+
+    def _step_groups(self, active, fail):
+        eng = self.engine
+        moved = False
+        buckets = {}
+        for job in active:
+            if job.cancel or job.phase not in ('fwd', 'adj_init', 'adj'):
+                continue
+            ph = 'fwd_init' if (job.phase == 'fwd' and job.init) else job.phase
+            buckets.setdefault((job.key, ph), []).append(job)
+        for (key, ph), jobs in buckets.items():
+            n = eng.slots(key)
+            for i in range(0, len(jobs), n):
+                part = jobs[i:i + n]
+                moved = True
+                try:
+                    self._issue(ph, part)
+                except Exception as e:
+                    if len(part) == 1 or not getattr(e, 'before_launch', False):
+                        for job in part:
+                            fail(job, f'{type(e).__name__}: {e}')
+                        continue
+                    # a rejected batch launched nothing: find the culprit alone
+                    for job in part:
+                        try:
+                            self._issue(ph, [job])
+                        except Exception as e1:
+                            fail(job, f'{type(e1).__name__}: {e1}')
+        return moved
+
+    def _issue(self, ph, jobs):
+        eng = self.engine
+        if ph == 'adj_init':
+            eng.adj_init(jobs)
+            for job in jobs:
+                job.phase, job.i = 'adj', 0
+            return
+        left = min(job.req.steps - job.i for job in jobs)
+        k = min(STEP_CHUNK, left)
+        if ph in ('fwd', 'fwd_init'):
+            eng.fwd(jobs, ph == 'fwd_init', k)
+            for job in jobs:
+                job.init = False
+                job.i += k
+                if job.i == job.req.steps:
+                    job.phase = 'objective'
+        else:
+            eng.adj(jobs, k)
+            for job in jobs:
+                job.i += k
+                if job.i == job.req.steps:
+                    job.phase = 'backprop'
+
+
+class BatchRejected(_lib.PmxError):
+    """A batched call refused on the host before anything was launched."""
+    before_launch = True
+
+
+class GpuEngine:
+    """Device work of the scheduler.  Per request: setup, objective and
+    backprop on the request's own CUDA stream.  Groups whose mesh the fused
+    x pass covers share one batched workspace (``slots`` simulations) and
+    one stream, and advance through the batched entry points; other meshes,
+    and every mesh with ``batch=False`` (the plain path), run one
+    simulation per call through the single-simulation entry points, on the
+    request's stream with a workspace of its own."""
+
+    def __init__(self, device=None, budget_bytes=150e9, batch=True):
+        self.dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
+        self.budget = budget_bytes
+        self.batch = batch
+        self.group_ws = {}           # key -> batched workspace
+        self.streams = {}            # key -> group stream
+        self.free = {}               # key -> free single workspaces
         self.lock = threading.Lock()
 
-    def acquire(self, mesh, dev):
-        key = (dev, tuple(mesh))
+    # ---- groups ----
+    def slots(self, key):
+        return group_slots(key[0], self.budget) if self.batch else 1
+
+    def group_bytes(self, key):
+        s = self.slots(key)
+        return s * workspace_bytes(key[0]) if s > 1 else 0
+
+    def job_bytes(self, req):
+        key = (req.ptcl_side * req.mesh_factor, req.ptcl_spacing / req.mesh_factor)
+        own = workspace_bytes(key[0]) if self.slots(key) == 1 else 0
+        return request_bytes(req.ptcl_side, req.grad) + own
+
+    def _group(self, key):
         with self.lock:
-            lst = self.free.get(key)
-            if lst:
-                return lst.pop()
-        return _lib.Workspace(mesh, adjoint=True, device=dev)
+            ws = self.group_ws.get(key)
+            st = self.streams.get(key)
+        if ws is None:
+            ws = _lib.Workspace((key[0],) * 3, adjoint=True, device=self.dev.index,
+                                slots=self.slots(key))
+            st = torch.cuda.Stream(device=self.dev)
+            with self.lock:
+                self.group_ws[key] = ws
+                self.streams[key] = st
+        return ws, st
 
-    def release(self, ws):
-        key = (ws.device.index, ws.mesh_shape)
+    def _single_ws(self, job):
+        d = job.dev
+        if 'ws' not in d:
+            with self.lock:
+                lst = self.free.get(job.key)
+                ws = lst.pop() if lst else None
+            if ws is None:
+                ws = _lib.Workspace((job.key[0],) * 3, adjoint=True, device=self.dev.index)
+            d['ws'] = ws
+        return d['ws']
+
+    def drop(self, key):
+        torch.cuda.synchronize(self.dev)
         with self.lock:
-            self.free.setdefault(key, []).append(ws)
+            self.group_ws.pop(key, None)
+            self.streams.pop(key, None)
+            self.free.pop(key, None)
 
-    def drop(self):
-        with self.lock:
-            self.free.clear()
+    def synchronize(self):
+        torch.cuda.synchronize(self.dev)
 
-
-class _Job:
-    """One request as a step-wise state machine on its own CUDA stream:
-    setup -> forward steps -> objective -> adjoint steps -> host backprop ->
-    done."""
-
-    def __init__(self, req, dev, pool):
-        self.req = req
-        self.dev = dev
-        self.pool = pool
-        self.stream = torch.cuda.Stream(device=dev)
-        side = req.ptcl_side
-        self.conf = Configuration(req.ptcl_spacing, (side,) * 3, req.mesh_factor,
-                                  a_nbody_maxstep=(1 - 1 / 64) / req.steps)
-        self.phase = 'setup'
-        self.i = 0
-        self.event = None
-        self.setup_future = None
-
-    # ---- host + device preparation (runs on a worker thread) ----
-    def setup(self):
+    # ---- per request ----
+    def setup(self, job):
+        """Host tables, white noise, 2LPT (on the request's own stream)."""
         torch.cuda.set_device(self.dev)
-        r, conf = self.req, self.conf
+        r = job.req
+        conf = Configuration(r.ptcl_spacing, (r.ptcl_side,) * 3, r.mesh_factor,
+                             a_nbody_maxstep=(1 - 1 / 64) / r.steps)
+        d = job.dev = {'conf': conf, 'stream': torch.cuda.Stream(device=self.dev), 'event': None}
         c = dict(r.cosmo)
         if 'sigma8' in c:
             s8 = c.pop('sigma8')
@@ -146,222 +439,216 @@ class _Job:
             c['A_s_1e9'] = float(base.A_s_1e9)
         cosmo = Cosmology(conf, **c)
         if r.grad:
-            self.Om_leaf = cosmo.Omega_m.clone().requires_grad_(True)
-            cosmo = cosmo.replace(Omega_m=self.Om_leaf)
+            d['Om_leaf'] = cosmo.Omega_m.clone().requires_grad_(True)
+            cosmo = cosmo.replace(Omega_m=d['Om_leaf'])
         cosmo = boltzmann(cosmo, conf, varlin=False)
-        self.cosmo = cosmo
-        self.ws = self.pool.acquire(conf.mesh_shape, self.dev.index)
-        with torch.cuda.stream(self.stream):
+        with torch.cuda.stream(d['stream']):
             modes = white_noise(r.seed, conf, real=True, device=self.dev)
             if r.grad:
                 modes.requires_grad_(True)
-                self.modes = modes
+                d['modes'] = modes
             with torch.set_grad_enabled(r.grad):
                 ptcl, _ = lpt(linear_modes(modes, cosmo, conf), cosmo, conf)
-            self.ptcl0 = ptcl
-            self.pmid = ptcl.pmid.contiguous()
-            self.disp = ptcl.disp.detach().contiguous().clone()
-            self.vel = ptcl.vel.detach().contiguous().clone()
-            self.acc = torch.empty_like(self.disp)
+            d['ptcl0'] = ptcl
+            d['pmid'] = ptcl.pmid.contiguous()
+            d['disp'] = ptcl.disp.detach().contiguous().clone()
+            d['vel'] = ptcl.vel.detach().contiguous().clone()
+            d['acc'] = torch.empty_like(d['disp'])
         fwd = _nb.op_factors(_nb.forward_ops(conf), cosmo, conf).detach()
-        self.f_fwd = fwd.to(torch.float32).numpy().reshape(-1, 3)
+        d['f_fwd'] = np.ascontiguousarray(fwd.to(torch.float32).numpy().reshape(-1, 3))
         if r.grad:
-            self.adj = _nb.op_factors(_nb.adjoint_ops(conf), cosmo, conf)
-            self.f_adj = self.adj.detach().to(torch.float32).numpy().reshape(-1, 3)
-        self.spec = _lib.make_spec(3, conf.mesh_shape, conf.mesh_shape, conf.cell_size)
-        self.Om = float(torch.as_tensor(cosmo.Omega_m).detach())
+            d['adj'] = _nb.op_factors(_nb.adjoint_ops(conf), cosmo, conf)
+            d['f_adj'] = np.ascontiguousarray(
+                d['adj'].detach().to(torch.float32).numpy().reshape(-1, 3))
+        d['spec'] = _lib.make_spec(3, conf.mesh_shape, conf.mesh_shape, conf.cell_size)
+        d['Om'] = float(torch.as_tensor(cosmo.Omega_m).detach())
+        d['event'] = self._record(d['stream'])
+
+    def _record(self, stream):
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        return ev
+
+    def idle(self, job):
+        d = job.dev
+        return d is None or d.get('event') is None or d['event'].query()
+
+    def _sim(self, job, factors, dots):
+        d = job.dev
+        return _lib.PmxSim(d['pmid'].data_ptr(), d['disp'].data_ptr(), d['vel'].data_ptr(),
+                           d['acc'].data_ptr(),
+                           d['disp_cot'].data_ptr() if 'disp_cot' in d else None,
+                           d['vel_cot'].data_ptr() if 'vel_cot' in d else None,
+                           d['alpha'].data_ptr() if 'alpha' in d else None,
+                           d['pmid'].shape[0], d['conf'].ptcl_num, d['Om'],
+                           None if factors is None else factors.ctypes.data,
+                           None if dots is None else dots.data_ptr())
+
+    def _call(self, jobs, name, tables, init, k):
+        """One batched call of the group's jobs on the group stream, after
+        each job's last work; records the jobs' new event."""
+        ws, st = self._group(jobs[0].key)
+        for job in jobs:
+            if job.dev['event'] is not None:
+                st.wait_event(job.dev['event'])
+        arr = (_lib.PmxSim * len(jobs))(*tables)
         lib = _lib.load()
+        status = getattr(lib, name)(ws.handle, jobs[0].dev['spec'], len(jobs), arr, int(init),
+                                    int(k), _lib.c_p(st.cuda_stream))
+        if status != 0:
+            msg = lib.pmx_last_error().decode(errors='replace')
+            cls = BatchRejected if status in (-1, -2, -3) else _lib.PmxError
+            raise cls(f'{name} failed with status {status}: {msg}')
+        ev = self._record(st)
+        for job in jobs:
+            job.dev['event'] = ev
+
+    def _single(self, job, fn):
+        """fn(lib, ws, stream pointer) on the request's own stream and workspace."""
+        d = job.dev
+        ws = self._single_ws(job)
+        st = d['stream']
+        if d['event'] is not None:
+            st.wait_event(d['event'])
+        fn(_lib.load(), ws, _lib.c_p(st.cuda_stream))
+        d['event'] = self._record(st)
+
+    def _batched(self, jobs):
+        return self.slots(jobs[0].key) > 1
+
+    def fwd(self, jobs, init, k):
+        keep = [np.ascontiguousarray(j.dev['f_fwd'][j.i:j.i + k]) for j in jobs]
+        if self._batched(jobs):
+            self._call(jobs, 'pmx_nbody_steps_batch',
+                       [self._sim(j, f, None) for j, f in zip(jobs, keep)], init, k)
+            return
         P = _lib.ptr
-        _lib.check(lib.pmx_force(self.ws.handle, self.spec, P(self.pmid), P(self.disp),
-                                 self.pmid.shape[0], conf.ptcl_num, self.Om, P(self.acc),
-                                 _lib.c_p(self.stream.cuda_stream)), 'pmx_force')
+        for j, f in zip(jobs, keep):
+            d = j.dev
+            n, N = d['pmid'].shape[0], d['conf'].ptcl_num
 
-    def start(self, executor):
-        self.setup_future = executor.submit(self.setup)
+            def run(lib, ws, st, d=d, f=f, n=n, N=N):
+                if init:
+                    _lib.check(lib.pmx_force(ws.handle, d['spec'], P(d['pmid']), P(d['disp']), n,
+                                             N, d['Om'], P(d['acc']), st), 'pmx_force')
+                _lib.check(lib.pmx_nbody_steps(ws.handle, d['spec'], P(d['pmid']), P(d['disp']),
+                                               P(d['vel']), P(d['acc']), n, N, k,
+                                               f.ctypes.data_as(ctypes.c_void_p), d['Om'], st),
+                           'pmx_nbody_steps')
+            self._single(j, run)
 
-    # ---- one unit of device work per call ----
-    def advance(self):
-        """Issues the job's next unit of work; returns False when it has to
-        wait (host setup or a device event still running)."""
-        if self.phase == 'setup':
-            if not self.setup_future.done():
-                return False
-            self.setup_future.result()      # re-raises setup errors
-            self.phase = 'fwd'
-            return True
-        lib = _lib.load()
+    def adj_init(self, jobs):
+        if self._batched(jobs):
+            self._call(jobs, 'pmx_nbody_adj_steps_batch',
+                       [self._sim(j, None, j.dev['dd'][-1]) for j in jobs], 1, 0)
+            return
         P = _lib.ptr
-        st = _lib.c_p(self.stream.cuda_stream)
-        n = self.pmid.shape[0]
-        conf = self.conf
-        if self.phase == 'fwd':
-            k = min(STEP_CHUNK, self.f_fwd.shape[0] - self.i)
-            fac = np.ascontiguousarray(self.f_fwd[self.i:self.i + k])
-            _lib.check(lib.pmx_nbody_steps(self.ws.handle, self.spec, P(self.pmid), P(self.disp),
-                                           P(self.vel), P(self.acc), n, conf.ptcl_num, k,
-                                           fac.ctypes.data_as(ctypes.c_void_p), self.Om, st),
-                       'pmx_nbody_steps')
-            self.i += k
-            if self.i == self.f_fwd.shape[0]:
-                self.phase = 'objective'
-            return
-        if self.phase == 'objective':
-            with torch.cuda.stream(self.stream):
-                disp = self.disp.clone().requires_grad_(self.req.grad)
-                dens = scatter(Particles(conf, self.pmid, disp), conf)
-                obj = (dens - 1).square().sum()
-                self.obj_dev = obj.detach()
-                self.rms_dev = self.disp.square().mean().sqrt()
-                if self.req.grad:
-                    (self.disp_cot,) = torch.autograd.grad(obj, disp)
-                    self.vel_cot = torch.zeros_like(self.vel)
-                    self.alpha = torch.zeros_like(self.disp)
-                    nsteps = self.f_adj.shape[0]
-                    self.dd = torch.zeros((nsteps + 1, 4), dtype=torch.float64, device=self.dev)
-            if not self.req.grad:
-                self._finish()
-                return
-            _lib.check(lib.pmx_force_vjp(self.ws.handle, self.spec, P(self.pmid), P(self.disp), n,
-                                         conf.ptcl_num, self.Om, P(self.vel_cot), P(self.acc),
-                                         P(self.alpha), P(self.dd[-1, 3:]), st), 'pmx_force_vjp')
-            self.phase = 'adj'
-            self.i = 0
-            return
-        if self.phase == 'adj':
-            k = min(STEP_CHUNK, self.f_adj.shape[0] - self.i)
-            fac = np.ascontiguousarray(self.f_adj[self.i:self.i + k])
-            _lib.check(lib.pmx_nbody_adj_steps(self.ws.handle, self.spec, P(self.pmid),
-                                               P(self.disp), P(self.vel), P(self.acc),
-                                               P(self.disp_cot), P(self.vel_cot), P(self.alpha),
-                                               n, conf.ptcl_num, k,
-                                               fac.ctypes.data_as(ctypes.c_void_p), self.Om,
-                                               P(self.dd[self.i]), st), 'pmx_nbody_adj_steps')
-            self.i += k
-            if self.i == self.f_adj.shape[0]:
-                self.host_dd = torch.empty(self.dd.shape, dtype=torch.float64, pin_memory=True)
-                with torch.cuda.stream(self.stream):
-                    self.host_dd.copy_(self.dd, non_blocking=True)
-                self.event = torch.cuda.Event()
-                self.event.record(self.stream)
-                self.phase = 'adj_wait'
-            return
-        if self.phase == 'adj_wait':
-            if not self.event.query():
-                return False
-            self._backprop()
-            self._finish()
-            return True
-        return False  # done_wait
+        for j in jobs:
+            d = j.dev
 
-    def _backprop(self):
+            def run(lib, ws, st, d=d):
+                _lib.check(lib.pmx_force_vjp(ws.handle, d['spec'], P(d['pmid']), P(d['disp']),
+                                             d['pmid'].shape[0], d['conf'].ptcl_num, d['Om'],
+                                             P(d['vel_cot']), P(d['acc']), P(d['alpha']),
+                                             P(d['dd'][-1, 3:]), st), 'pmx_force_vjp')
+            self._single(j, run)
+
+    def adj(self, jobs, k):
+        keep = [np.ascontiguousarray(j.dev['f_adj'][j.i:j.i + k]) for j in jobs]
+        if self._batched(jobs):
+            self._call(jobs, 'pmx_nbody_adj_steps_batch',
+                       [self._sim(j, f, j.dev['dd'][j.i]) for j, f in zip(jobs, keep)], 0, k)
+            return
+        P = _lib.ptr
+        for j, f in zip(jobs, keep):
+            d = j.dev
+            i0 = j.i
+
+            def run(lib, ws, st, d=d, f=f, i0=i0):
+                _lib.check(lib.pmx_nbody_adj_steps(
+                    ws.handle, d['spec'], P(d['pmid']), P(d['disp']), P(d['vel']), P(d['acc']),
+                    P(d['disp_cot']), P(d['vel_cot']), P(d['alpha']), d['pmid'].shape[0],
+                    d['conf'].ptcl_num, k, f.ctypes.data_as(ctypes.c_void_p), d['Om'],
+                    P(d['dd'][i0]), st), 'pmx_nbody_adj_steps')
+            self._single(j, run)
+
+    def objective(self, job):
+        """Objective sum((rho - 1)^2) at a = 1 and, for gradients, its
+        cotangent of disp (the adjoint's initial disp_cot)."""
+        d, r = job.dev, job.req
+        conf = d['conf']
+        st = d['stream']
+        st.wait_event(d['event'])
+        with torch.cuda.stream(st):
+            disp = d['disp'].clone().requires_grad_(r.grad)
+            dens = scatter(Particles(conf, d['pmid'], disp), conf)
+            obj = (dens - 1).square().sum()
+            d['obj'] = obj.detach()
+            d['rms'] = d['disp'].square().mean().sqrt()
+            if r.grad:
+                (d['disp_cot'],) = torch.autograd.grad(obj, disp)
+                d['vel_cot'] = torch.zeros_like(d['vel'])
+                d['alpha'] = torch.zeros_like(d['disp'])
+                d['dd'] = torch.zeros((r.steps + 1, 4), dtype=torch.float64, device=self.dev)
+        d['event'] = self._record(st)
+
+    def backprop(self, job):
         """Chain the adjoint's results to the white-noise modes and Omega_m:
         initial-state cotangents through 2LPT/linear_modes (autograd), factor
         sensitivities through the float64 factor functions, plus the direct
         Omega_m term of every force (nbody.py:80-99)."""
-        dd = self.host_dd
-        nsteps = self.f_adj.shape[0]
+        d = job.dev
+        dd = d['dd'].cpu()
+        nsteps = d['f_adj'].shape[0]
         dots = dd[:nsteps, :3].reshape(-1)
         om_force = torch.cat((dd[nsteps:, 3], dd[:nsteps, 3]))
-        f64 = torch.tensor(self.f_adj, dtype=torch.float64)
+        f64 = torch.tensor(d['f_adj'], dtype=torch.float64)
         om_direct = -(om_force[:nsteps] * f64[:, 0]).sum() - (om_force[1:] * f64[:, 2]).sum()
-        with torch.cuda.stream(self.stream):
-            torch.autograd.backward([self.ptcl0.disp, self.ptcl0.vel, self.adj],
-                                    [self.disp_cot, self.vel_cot, -dots])
-        self.grad_rms = self.modes.grad.square().mean().sqrt()
-        self.dobj_dOm = self.Om_leaf.grad + om_direct
+        st = d['stream']
+        st.wait_event(d['event'])
+        with torch.cuda.stream(st):
+            torch.autograd.backward([d['ptcl0'].disp, d['ptcl0'].vel, d['adj']],
+                                    [d['disp_cot'], d['vel_cot'], -dots])
+        d['grad_rms'] = d['modes'].grad.square().mean().sqrt()
+        d['dobj_dOm'] = d['Om_leaf'].grad + om_direct
+        d['event'] = self._record(st)
 
-    def _finish(self):
-        self.event = torch.cuda.Event()
-        self.event.record(self.stream)
-        self.phase = 'done_wait'
+    def result(self, job):
+        d, g = job.dev, job.req.grad
+        return Result(job.req.rid, None, float(d['rms']), float(d['obj']),
+                      float(d['grad_rms']) if g else None, float(d['dobj_dOm']) if g else None)
 
-    def ready(self):
-        return self.phase == 'done_wait' and self.event.query()
-
-    def result(self):
-        g = self.req.grad
-        return Result(self.req.rid, None, float(self.rms_dev), float(self.obj_dev),
-                      float(self.grad_rms) if g else None, float(self.dobj_dOm) if g else None)
+    def release(self, job):
+        d = job.dev
+        if d is not None and 'ws' in d:
+            with self.lock:
+                self.free.setdefault(job.key, []).append(d['ws'])
+        job.dev = None
 
 
 class Server:
     """Continuous batching with HBM admission (see the module docstring)."""
 
-    def __init__(self, budget_bytes=150e9, max_jobs=64, device=None, host_workers=4):
-        self.budget = budget_bytes
-        self.max_jobs = max_jobs
-        self.dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
-        self.pool = WorkspacePool()
-        self.host_workers = host_workers
+    def __init__(self, budget_bytes=150e9, max_jobs=64, device=None, host_workers=4, batch=True):
+        self.engine = GpuEngine(device, budget_bytes, batch)
+        self.sched = Scheduler(self.engine, budget_bytes, max_jobs, host_workers)
 
     def cost(self, req):
-        return (request_bytes(req.ptcl_side, req.grad)
-                + workspace_bytes(req.ptcl_side * req.mesh_factor))
+        return self.sched.cost(req)
 
-    def run(self, requests, realtime=True):
-        """Serve ``requests`` (arrival offsets in seconds; realtime=False
-        makes all available at t = 0).  Returns (results in request order,
-        stats)."""
-        pending = sorted(requests, key=lambda r: r.arrival)
-        qi = 0
-        waiting, active = [], []
-        used = 0.0
-        results = {}
-        ex = ThreadPoolExecutor(max_workers=self.host_workers)
-        t0 = time.perf_counter()
-        try:
-            while qi < len(pending) or waiting or active:
-                now = time.perf_counter() - t0
-                while qi < len(pending) and (not realtime or pending[qi].arrival <= now):
-                    waiting.append(pending[qi])
-                    qi += 1
-                while waiting and len(active) < self.max_jobs:
-                    c = self.cost(waiting[0])
-                    if used + c > self.budget and active:
-                        break
-                    req = waiting.pop(0)
-                    job = _Job(req, self.dev, self.pool)
-                    job.cost = c
-                    job.t_arr = req.arrival if realtime else 0.0
-                    job.start(ex)
-                    used += c
-                    active.append(job)
-                if not active:
-                    if qi < len(pending):
-                        time.sleep(max(0.0, min(0.002, pending[qi].arrival - now)))
-                    continue
-                moved = False
-                for job in list(active):
-                    if job.advance() is not False:
-                        moved = True
-                    if job.ready():
-                        moved = True
-                        res = job.result()
-                        res.latency = (time.perf_counter() - t0) - job.t_arr
-                        results[job.req.rid] = res
-                        self.pool.release(job.ws)
-                        used -= job.cost
-                        active.remove(job)
-                if not moved:
-                    # every job waits on host setup or the device: yield the
-                    # GIL to the setup threads instead of spinning
-                    time.sleep(2e-4)
-        finally:
-            ex.shutdown(wait=True)
-        torch.cuda.synchronize(self.dev)
-        wall = time.perf_counter() - t0
-        lat = np.array([r.latency for r in results.values()])
-        stats = {'sims': len(results), 'wall_s': wall, 'sims_per_s': len(results) / wall,
-                 'p50_s': float(np.percentile(lat, 50)) if len(lat) else None,
-                 'p99_s': float(np.percentile(lat, 99)) if len(lat) else None}
-        return [results[r.rid] for r in requests], stats
+    def cancel(self, rid):
+        self.sched.cancel(rid)
+
+    def run(self, requests, realtime=True, on_turn=None):
+        return self.sched.run(requests, realtime, on_turn)
 
 
 def run_sequential(requests, device=None):
     """The plain path: the same requests one at a time, each to completion
-    (one job, no overlap) -- the baseline the served form is compared to."""
-    return Server(budget_bytes=float('inf'), max_jobs=1, device=device,
-                  host_workers=1).run(requests, realtime=False)
+    (one simulation per call, no overlap) -- the baseline the served form is
+    compared to."""
+    return Server(budget_bytes=float('inf'), max_jobs=1, device=device, host_workers=1,
+                  batch=False).run(requests, realtime=False)
 
 
 def make_stream(n, rate_hz, seed=0, sides=(64, 128, 256), factors=(1, 2), steps=(10, 100),

@@ -416,3 +416,65 @@ def test_window_deposit_equals_direct_atomics(cuda, shuffle):
     assert rel_l2(a1, a2) < 1e-6
     assert rel_l2(d1, d2) < 1e-5
     assert abs(o1 / o2 - 1) < 5e-5   # a float64 sum over ~1e5 float32 terms in any order
+
+
+@pytest.mark.parametrize('state', ['lattice', 'halos', 'shuffled_halos'])
+def test_aggregated_deposits_equal_direct_atomics(cuda, state):
+    """Warp-aggregated deposits (PMX_WS_AGG: lanes whose particles share a
+    base cell sum in shared memory, one lane reduces) against one atomic per
+    contribution: the force, its VJP and a multi-step forward + adjoint run.
+    'halos' pulls the particles into a few dense clumps (many lanes of a warp
+    share cells: the aggregated path), 'lattice' barely moves them (no shared
+    cells: the direct path of the same kernels)."""
+    import ctypes
+    oconf, gconf, pmid, disp, vel = make((32, 32, 32), 2, 1.0, 0.05)
+    if state != 'lattice':
+        pos = ics.pos(pmid, disp, oconf)
+        rng = np.random.default_rng(8)
+        centres = rng.uniform(0, oconf.box_size[0], (6, 3))
+        near = centres[np.argmin(((pos[:, None, :] - centres[None]) ** 2).sum(-1), axis=1)]
+        # 95% of the way to the nearest of six centres, plus a little scatter
+        pos = pos + 0.95 * (near - pos) + rng.normal(0, 0.3, pos.shape)
+        disp = (pos - pmid.astype(np.float64) * oconf.cell_size).astype(np.float32)
+        if state == 'shuffled_halos':
+            perm = rng.permutation(len(pmid))
+            pmid, disp, vel = pmid[perm], disp[perm], vel[perm]
+    cot = np.random.default_rng(6).normal(size=disp.shape).astype(np.float32)
+    gcos = pg.boltzmann(pg.SimpleLCDM(gconf), gconf)
+    fwd = gnb.op_factors(gnb.forward_ops(gconf), gcos, gconf).detach()
+    adj = gnb.op_factors(gnb.adjoint_ops(gconf), gcos, gconf).detach()
+    f_fwd = np.ascontiguousarray(fwd.to(torch.float32).numpy().reshape(-1, 3))[:4]
+    f_adj = np.ascontiguousarray(adj.to(torch.float32).numpy().reshape(-1, 3))[-4:]
+    out = []
+    for agg in (True, False):
+        ws = _lib.Workspace(gconf.mesh_shape, adjoint=True, agg=agg)
+        spec = _lib.make_spec(3, gconf.mesh_shape, gconf.mesh_shape, gconf.cell_size)
+        n, st = len(pmid), _lib.stream_ptr(cuda)
+        P, D, V = T(pmid, cuda), T(disp, cuda), T(vel, cuda)
+        acc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+        dc = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+        om = torch.zeros((), dtype=torch.float64, device=cuda)
+        _lib.call('pmx_force_vjp', ws.handle, spec, P, D, n, gconf.ptcl_num, 0.3, T(cot, cuda), acc,
+                  dc, om, st)
+        res = [acc.cpu().numpy(), dc.cpu().numpy(), float(om)]
+        A = torch.empty_like(D)
+        _lib.call('pmx_force', ws.handle, spec, P, D, n, gconf.ptcl_num, 0.3, A, st)
+        _lib.call('pmx_nbody_steps', ws.handle, spec, P, D, V, A, n, gconf.ptcl_num, 4,
+                  f_fwd.ctypes.data_as(ctypes.c_void_p), 0.3, st)
+        res.append(D.cpu().numpy())
+        vc, al = T(cot, cuda), torch.zeros_like(D)
+        dcot = torch.zeros_like(D)
+        dots = torch.zeros((4, 4), dtype=torch.float64, device=cuda)
+        _lib.call('pmx_nbody_adj_steps', ws.handle, spec, P, D, V, A, dcot, vc, al, n,
+                  gconf.ptcl_num, 4, f_adj.ctypes.data_as(ctypes.c_void_p), 0.3, dots, st)
+        res += [D.cpu().numpy(), vc.cpu().numpy()]
+        out.append(res)
+        del ws
+    (a1, d1, o1, x1, y1, v1), (a2, d2, o2, x2, y2, v2) = out
+    # one force: only the order of the float32 adds differs
+    assert rel_l2(a1, a2) < 1e-5
+    assert rel_l2(d1, d2) < 1e-4
+    assert abs(o1 / o2 - 1) < 1e-4
+    # 4 forward steps, then 4 reverse steps (which amplify the order noise)
+    assert rel_l2(x1, x2) < 1e-5 and rel_l2(y1, y2) < 1e-4
+    assert rel_l2(v1, v2) < 1e-3
