@@ -66,6 +66,8 @@ def parse():
                          'replica launch and the reduction over ranks on CPU (gloo)')
     ap.add_argument('--serve', type=int, default=0,
                     help='serving mode: number of requests of the serving stream')
+    ap.add_argument('--serve-requests', type=int, default=32,
+                    help='requests of the serving measurement in the default line (0: none)')
     ap.add_argument('--serve-sides', default='64,128,256')
     ap.add_argument('--contention', action='store_true',
                     help='scatter/gather contention stress: 256^3 particles, 256^3 mesh, 64 Mpc/h '
@@ -417,6 +419,7 @@ def run_pmx(args, rank, world, local_rank):
 
     # ---- e2e: the same step pair through the C ABI with host buffers ----
     e2e = None
+    dev_bufs = host = None
     if not args.no_e2e:
         dev_bufs = dict(pmid=pmid, disp=disp, vel=vel, acc=acc, disp_cot=disp_cot,
                         vel_cot=vel_cot, alpha=alpha)
@@ -507,6 +510,18 @@ def run_pmx(args, rank, world, local_rank):
                          f'{int(round(cs * args.mesh))}^3 mesh ({times[0]:.1f} s); FFTs on all '
                          f'cores, particle work single-threaded'}
 
+    # the serving stream (the metric's second half), after the large run's
+    # buffers are released
+    serve = None
+    if args.serve_requests > 0 and world == 1:
+        del pmid, disp, vel, acc, disp_cot, vel_cot, alpha, disp0, vel0, ws, seg_dots, dots
+        del dev_bufs, host
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        sides = tuple(int(s) for s in args.serve_sides.split(','))
+        steps_rng = tuple(int(s) for s in args.serve_steps.split(','))
+        serve = serving_measure(args.serve_requests, sides, steps_rng)
+
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms_step, 'higher_is_better': True,
@@ -528,6 +543,7 @@ def run_pmx(args, rank, world, local_rank):
         'full_run': None if full is None else dict(
             full, step_roofline_frac=step_bytes / (full['ms_per_step'] / 1e3) / 1e9 / peak),
         'clocks': clk,
+        'serving': serve,
     }
     print(json.dumps(line), flush=True)
 
@@ -609,32 +625,50 @@ def launch_replicas(args):
     return subprocess.call(cmd)
 
 
-def run_serve(args):
-    """Serving stream (mixed grids, mesh factors, step counts, cosmologies,
-    20% gradients) served with continuous batching vs one at a time, same
-    requests; then the served form under Poisson arrivals at 80% of its
-    throughput for p50/p99 latency."""
-    import torch
+def serving_measure(n, sides, steps, realtime=True):
+    """The serving stream (C5 distribution: particle grid from `sides`, mesh
+    factor 1 or 2, steps uniform in `steps`, random cosmologies, 20%
+    gradients) served with continuous batching and one at a time, the same
+    requests; each server is warmed first with one short request per mesh
+    group, so both are timed with their workspaces and plans in place.
+    Then the served form under Poisson arrivals at 80% of its throughput,
+    for p50/p99 latency."""
     from pmwd_gb300 import serving
+    reqs = serving.make_stream(n, rate_hz=0.0, seed=0, sides=sides, steps=steps)
+    warm = [serving.Request(1000 + i, s, f, 2, dict(sigma8=0.8, n_s=0.96, Omega_m=0.3,
+                                                     Omega_b=0.05, h=0.7), i, grad=True)
+            for i, (s, f) in enumerate((s, f) for s in sides for f in (1, 2))]
+    seq_srv = serving.sequential_server()
+    seq_srv.run(warm, realtime=False)
+    _, seq = seq_srv.run(reqs, realtime=False)
+    seq_srv.close()
+    srv = serving.Server(budget_bytes=150e9)
+    srv.run(warm, realtime=False)
+    _, st = srv.run(reqs, realtime=False)
+    out = {'served_sims_per_s': st['sims_per_s'], 'sequential_sims_per_s': seq['sims_per_s'],
+           'speedup_vs_sequential': st['sims_per_s'] / seq['sims_per_s'],
+           'failed': st['failed'] + seq['failed'], 'requests': n,
+           'workload': f'{n} requests, ptcl grid {sides}^3, mesh factor {{1,2}}, steps U{steps}, '
+                       f'20% gradients, HBM budget 150 GB, spacing 2 Mpc/h'}
+    if realtime:
+        rate = 0.8 * st['sims_per_s']
+        timed = serving.make_stream(n, rate_hz=rate, seed=0, sides=sides, steps=steps)
+        _, rt = srv.run(timed, realtime=True)
+        out.update({'poisson_rate_hz': rate, 'p50_s': rt['p50_s'], 'p99_s': rt['p99_s'],
+                    'realtime_sims_per_s': rt['sims_per_s']})
+    srv.close()
+    return out
+
+
+def run_serve(args):
+    """Serving mode of bench.py: serving_measure on --serve requests."""
+    import torch
     torch.cuda.set_device(0)
     sides = tuple(int(s) for s in args.serve_sides.split(','))
     steps = tuple(int(s) for s in args.serve_steps.split(','))
-    reqs = serving.make_stream(args.serve, rate_hz=0.0, seed=0, sides=sides, steps=steps)
-    warm = serving.make_stream(4, rate_hz=0.0, seed=1, sides=sides[:1], steps=(2, 3))
-    serving.run_sequential(warm)
-    _, seq = serving.run_sequential(reqs)
-    _, srv = serving.Server(budget_bytes=150e9).run(reqs, realtime=False)
-    rate = 0.8 * srv['sims_per_s']
-    timed = serving.make_stream(args.serve, rate_hz=rate, seed=0, sides=sides, steps=steps)
-    _, rt = serving.Server(budget_bytes=150e9).run(timed, realtime=True)
-    line = {'metric': 'served sims/s', 'value': srv['sims_per_s'], 'unit': 'sims/s',
-            'higher_is_better': True, 'n_gpus': 1,
-            'sequential_sims_per_s': seq['sims_per_s'],
-            'speedup_vs_sequential': srv['sims_per_s'] / seq['sims_per_s'],
-            'poisson_rate_hz': rate, 'p50_s': rt['p50_s'], 'p99_s': rt['p99_s'],
-            'realtime_sims_per_s': rt['sims_per_s'],
-            'config': {'workload': f'{args.serve} requests, ptcl grid {sides}^3, mesh factor '
-                                   f'{{1,2}}, steps U{steps}, 20% gradients, HBM budget 150 GB'}}
+    m = serving_measure(args.serve, sides, steps)
+    line = {'metric': 'served sims/s', 'value': m['served_sims_per_s'], 'unit': 'sims/s',
+            'higher_is_better': True, 'n_gpus': 1, **m, 'config': {'workload': m['workload']}}
     print(json.dumps(line), flush=True)
 
 

@@ -235,18 +235,31 @@ def linear_power(k, a, cosmo, conf):
     return Plin
 
 
-def varlin_integ(cosmo, conf):
+def varlin_integ(cosmo, conf, only=None):
     """Tabulate the linear variance in top-hat spheres at conf.varlin_R
     (boltzmann.py:272-291).  Direct quadrature over ln k replaces mcfit's
-    FFTLog transform."""
+    FFTLog transform.
+
+    ``only``: radii at which the table will be read; only the table entries
+    that linear interpolation at those radii uses are computed (each entry's
+    quadrature is independent of the others), the rest are left at zero."""
     lnk = torch.linspace(math.log(1e-5), math.log(1e3), 8001, dtype=DT)
     k = torch.exp(lnk)
     P = linear_power(k, None, cosmo, conf)
     R = conf.varlin_R
+    rows = None
+    if only is not None:
+        x = torch.as_tensor(only, dtype=DT).reshape(-1)
+        i = torch.clamp(torch.searchsorted(R, x, right=True), 1, len(R) - 1)
+        rows = torch.unique(torch.cat((i - 1, i)))
+        R = R[rows]
     x = k[None, :] * R[:, None]
     W = 3 * (torch.sin(x) - x * torch.cos(x)) / x ** 3
     integrand = k ** 3 * P * W ** 2 / (2 * math.pi ** 2)
     var = torch.trapezoid(integrand, lnk, dim=1)
+    if rows is not None:
+        full = torch.zeros(len(conf.varlin_R), dtype=var.dtype)
+        var = full.index_put((rows,), var)
     return cosmo.replace(varlin=var)
 
 

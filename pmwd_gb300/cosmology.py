@@ -89,9 +89,11 @@ class Cosmology:
     @classmethod
     def from_sigma8(cls, conf, sigma8, *args, **kwargs):
         """Cosmology with sigma8 instead of A_s (cosmology.py:95-105)."""
-        from .boltzmann import boltzmann
+        from .boltzmann import boltzmann, varlin_integ
         cosmo = cls(conf, 1, *args, **kwargs)
-        cosmo = boltzmann(cosmo, conf)
+        # only the variance entries around R = 8 Mpc/h are read
+        cosmo = boltzmann(cosmo, conf, varlin=False)
+        cosmo = varlin_integ(cosmo, conf, only=8 * conf.Mpc_SI / conf.L)
         A_s_1e9 = (sigma8 / cosmo.sigma8) ** 2
         return cls(conf, A_s_1e9, *args, **kwargs)
 

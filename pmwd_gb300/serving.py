@@ -147,7 +147,9 @@ class Scheduler:
       one call for jobs of one key, in the same phase (may raise);
     * engine.objective(job) / engine.backprop(job) (may raise);
     * engine.idle(job) -> nothing of the job is in flight on the device;
-    * engine.result(job) -> Result; engine.release(job); engine.drop(key).
+    * engine.result(job) -> Result; engine.release(job);
+    * engine.resident() -> keys whose group workspace exists; engine.drop(key)
+      frees one.
     """
 
     def __init__(self, engine, budget_bytes=150e9, max_jobs=64, host_workers=4):
@@ -177,8 +179,10 @@ class Scheduler:
         pending = sorted(requests, key=lambda r: r.arrival)
         qi = 0
         waiting, active = [], []
-        used = 0.0
-        groups = {}                 # key -> bytes charged for its workspace
+        # key -> bytes charged for its workspace (groups of earlier runs
+        # keep theirs until the budget needs the room)
+        groups = {k: eng.group_bytes(k) for k in eng.resident()}
+        used = float(sum(groups.values()))
         results = {}
         ex = ThreadPoolExecutor(max_workers=self.host_workers)
         t0 = time.perf_counter()
@@ -289,8 +293,6 @@ class Scheduler:
                     time.sleep(2e-4)
         finally:
             ex.shutdown(wait=True)
-            for k in list(groups):
-                eng.drop(k)
         eng.synchronize()
         wall = now()
         ok = [r for r in results.values() if r.error is None]
@@ -414,12 +416,24 @@ class GpuEngine:
             d['ws'] = ws
         return d['ws']
 
+    def resident(self):
+        with self.lock:
+            return list(self.group_ws)
+
     def drop(self, key):
         torch.cuda.synchronize(self.dev)
         with self.lock:
             self.group_ws.pop(key, None)
             self.streams.pop(key, None)
             self.free.pop(key, None)
+
+    def close(self):
+        """Frees every workspace the engine holds."""
+        torch.cuda.synchronize(self.dev)
+        with self.lock:
+            self.group_ws.clear()
+            self.streams.clear()
+            self.free.clear()
 
     def synchronize(self):
         torch.cuda.synchronize(self.dev)
@@ -642,13 +656,24 @@ class Server:
     def run(self, requests, realtime=True, on_turn=None):
         return self.sched.run(requests, realtime, on_turn)
 
+    def close(self):
+        self.engine.close()
 
-def run_sequential(requests, device=None):
-    """The plain path: the same requests one at a time, each to completion
-    (one simulation per call, no overlap) -- the baseline the served form is
+
+def sequential_server(device=None):
+    """The plain path: requests one at a time, each to completion (one
+    simulation per call, no overlap) -- the baseline the served form is
     compared to."""
     return Server(budget_bytes=float('inf'), max_jobs=1, device=device, host_workers=1,
-                  batch=False).run(requests, realtime=False)
+                  batch=False)
+
+
+def run_sequential(requests, device=None):
+    srv = sequential_server(device)
+    try:
+        return srv.run(requests, realtime=False)
+    finally:
+        srv.close()
 
 
 def make_stream(n, rate_hz, seed=0, sides=(64, 128, 256), factors=(1, 2), steps=(10, 100),

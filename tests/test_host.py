@@ -172,3 +172,16 @@ def test_growth_ode_einstein_de_sitter_is_exact():
     assert lib.pmx_growth_ode(f(prm), 1, f(lna), 40, 1e-11, 1e-13, f(y), f(dy)) == 0
     np.testing.assert_allclose(y[:, 0, :], np.tile([1.0, 0.0, 3 / 7, 0.0], (40, 1)), atol=1e-12)
     np.testing.assert_allclose(dy[:, 0, :], 0.0, atol=1e-12)
+
+
+def test_from_sigma8_reads_only_the_entries_it_needs():
+    """Cosmology.from_sigma8 integrates the variance only at the two table
+    radii around 8 Mpc/h; sigma8 interpolates between exactly those, so
+    A_s equals the one from the whole table (cosmology.py:95-105)."""
+    import pmwd_gb300 as pg
+    from pmwd_gb300.boltzmann import boltzmann
+    conf = pg.Configuration(2.0, (16,) * 3, 2)
+    for s8, om in ((0.8, 0.3), (0.72, 0.21), (0.89, 0.39)):
+        fast = pg.Cosmology.from_sigma8(conf, s8, n_s=0.96, Omega_m=om, Omega_b=0.05, h=0.7)
+        full = boltzmann(pg.Cosmology(conf, 1, n_s=0.96, Omega_m=om, Omega_b=0.05, h=0.7), conf)
+        assert abs(float(fast.A_s_1e9) / float((s8 / full.sigma8) ** 2) - 1) < 1e-12

@@ -107,6 +107,9 @@ class FakeEngine:
         self.released.append(job.req.rid)
         job.dev = None
 
+    def resident(self):
+        return []
+
     def drop(self, key):
         self.dropped.append(key)
 
@@ -206,7 +209,9 @@ def test_results_same_alone_and_in_mix(cuda):
                                steps=(4, 8), grad_frac=0.5)
     reqs[0].grad = True
     alone, st_seq = serving.run_sequential(reqs)
-    mixed, st_mix = serving.Server(budget_bytes=8e9, max_jobs=8).run(reqs, realtime=False)
+    srv = serving.Server(budget_bytes=8e9, max_jobs=8)
+    mixed, st_mix = srv.run(reqs, realtime=False)
+    srv.close()
     assert st_mix['sims'] == len(reqs) == st_seq['sims']
     for a, m in zip(alone, mixed):
         assert a.rid == m.rid
@@ -230,6 +235,7 @@ def test_results_same_alone_and_in_one_batched_group(cuda):
     srv = serving.Server(budget_bytes=8e9, max_jobs=8)
     assert srv.engine.slots((64, 1.0)) > 1
     mixed, st = srv.run(reqs, realtime=False)
+    srv.close()
     assert st['sims'] == 5 and st['failed'] == 0
     # d obj / d Omega_m sums the force sensitivity over every step: the order
     # of the float32 atomic adds moves a reconstructed particle across a CIC
