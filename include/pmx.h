@@ -134,6 +134,10 @@ typedef struct pmx_workspace pmx_workspace;
                               directly instead of replaying captured graphs */
 #define PMX_WS_PLANE16 64  /* plane kernels in clusters of 16 CTAs (the
                               non-portable size) instead of 8 */
+#define PMX_WS_TMA 256     /* forward gathers stage each warp's box of the
+                              acceleration meshes in shared memory with one
+                              cp.async.bulk.tensor copy (fused x-pass path,
+                              n2 % 4 == 0, single-simulation workspaces) */
 #define PMX_WS_AGG 128     /* warp-aggregated deposits: lanes whose particles
                               share a cell sum their contributions in shared
                               memory and one lane issues the reductions
@@ -318,6 +322,11 @@ typedef struct pmx_sim {
 int pmx_workspace_create_batch(const int64_t mesh_shape[3], int32_t flags,
                                int32_t slots, pmx_workspace **ws);
 int pmx_workspace_slots(const pmx_workspace *ws, int32_t *slots);
+
+/* *gave_up = 1 if a TMA-staged gather of this workspace ever stopped waiting
+ * for its copy (it then read global memory; results stay correct).  Waits
+ * for the device. */
+int pmx_workspace_tma_status(pmx_workspace *ws, int32_t *gave_up);
 
 /* For each of the nsim simulations (nsim <= slots): with init_force, first
  * acc = F(disp) as pmx_force; then nsteps steps as pmx_nbody_steps. */

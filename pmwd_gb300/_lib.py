@@ -54,6 +54,7 @@ SIGNATURES = {
     'pmx_workspace_create_batch': (c_int, [ctypes.POINTER(c_i64), c_i32, c_i32,
                                            ctypes.POINTER(c_p)]),
     'pmx_workspace_slots': (c_int, [c_p, ctypes.POINTER(c_i32)]),
+    'pmx_workspace_tma_status': (c_int, [c_p, ctypes.POINTER(c_i32)]),
     'pmx_nbody_steps_batch': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_i32,
                                       ctypes.POINTER(PmxSim), c_i32, c_i32, c_p]),
     'pmx_nbody_adj_steps_batch': (c_int, [c_p, ctypes.POINTER(EnmeshSpec), c_i32,
@@ -116,6 +117,7 @@ PMX_WS_VEC = 16
 PMX_WS_NO_GRAPH = 32
 PMX_WS_PLANE16 = 64
 PMX_WS_AGG = 128
+PMX_WS_TMA = 256
 PMX_WS_CHAINS_SHIFT = 8
 PMX_WS_SLAB_SHIFT = 12
 
@@ -197,12 +199,12 @@ class Workspace:
 
     def __init__(self, mesh_shape, adjoint=True, device=None, cufft3d=False, window=False,
                  plane=False, vec=False, graphs=True, plane16=False, chains=0, slab_log2=0,
-                 slots=1, agg=False):
+                 slots=1, agg=False, tma=False):
         """Flags of pmx_workspace_create (include/pmx.h): ``cufft3d`` 3-D
         cuFFT plans instead of the fused x pass, ``window`` warp-window
         deposits, ``plane`` cluster plane kernels (``plane16``: clusters of
         16), ``vec`` vector z-pair reductions, ``agg`` warp-aggregated
-        deposits, ``graphs`` slab loops as CUDA
+        deposits, ``tma`` TMA-staged forward gathers, ``graphs`` slab loops as CUDA
         graphs, ``chains`` concurrent slab chains and ``slab_log2`` planes
         per cuFFT execution (0: defaults).  ``slots`` > 1: a batched
         workspace for that many simulations of this mesh shape
@@ -214,6 +216,7 @@ class Workspace:
                  | (PMX_WS_WINDOW if window else 0) | (PMX_WS_PLANE if plane else 0)
                  | (PMX_WS_VEC if vec else 0) | (0 if graphs else PMX_WS_NO_GRAPH)
                  | (PMX_WS_PLANE16 if plane16 else 0) | (PMX_WS_AGG if agg else 0)
+                 | (PMX_WS_TMA if tma else 0)
                  | ((int(chains) & 7) << PMX_WS_CHAINS_SHIFT)
                  | ((int(slab_log2) & 15) << PMX_WS_SLAB_SHIFT))
         self.device = torch.device('cuda', torch.cuda.current_device() if device is None else device)

@@ -16,6 +16,8 @@
 //   part  4 * PMAX    float64 per-block partial sums of the dot products
 // with M = n0*n1*n2 and Mc = n0*n1*(n2/2+1).
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cufft.h>
 
 #include <cmath>
@@ -113,6 +115,9 @@ struct pmx_workspace {
     bool plane16 = false;       // clusters of 16 CTAs instead of 8
     bool vec = false;           // vector z-pair reductions (n2 % 4 == 0)
     bool agg = false;           // warp-aggregated deposits
+    bool tma = false;           // TMA-staged forward gathers (tmap describes g)
+    CUtensorMap tmap;
+    int *err = nullptr;         // device word: a TMA wait gave up (kernels then read global)
     float2 *ptw = nullptr;      // plane_twiddles(n1, n2)
     float2 *pscr = nullptr;     // c2r scratch: one n1 x n2p plane per cluster
     int pcl = 0;                // clusters the scratch serves
@@ -659,6 +664,132 @@ __global__ void __launch_bounds__(PT) k_kds(Hot h, const int16_t *__restrict__ p
                                             float *vel, const float *__restrict__ acc, int64_t n,
                                             float K1, float D, float *dens) {
     kds_body<KD, WIN, KAHAN, AGG>(h, pmid, disp, vel, acc, n, K1, D, dens);
+}
+
+// ---------------------------------------------------------------------------
+// TMA-staged gather (workspaces with PMX_WS_TMA, plane-interleaved meshes).
+// Each warp takes 32 consecutive particles; their lower neighbour cells span
+// a small box of the (x, 3, n1, n2) acceleration meshes (Lagrangian order:
+// one z row of the particle grid).  One lane loads that box -- TBX x-planes
+// x 3 components x TBY rows x TBZ cells -- into the warp's shared-memory
+// buffer with one cp.async.bulk.tensor copy completing on an mbarrier, and
+// the 8-point interpolation then reads shared memory.  A warp whose cells do
+// not fit the box, or whose box would cross the periodic boundary (the
+// copy fills out-of-range cells with zeros), reads global memory instead, as
+// k_gather3 does; both paths add the same products in the same order.
+// ---------------------------------------------------------------------------
+
+constexpr int TBX = 3, TBY = 3, TBZ = 72;            // box: x-planes, y rows, z cells
+constexpr int TBOX = TBX * 3 * TBY * TBZ;            // floats a box copy writes
+constexpr int TBOX_PAD = (TBOX + 31) & ~31;          // box stride: 128-byte aligned
+constexpr size_t TMA_SMEM = (PT / 32) * (TBOX_PAD * 4 + 8);
+constexpr int TMA_WAIT_LIMIT = 1 << 24;              // mbarrier polls before giving up
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+// Waits for the mbarrier phase `parity`; false after TMA_WAIT_LIMIT polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+    const unsigned a = smem_addr(bar);
+    for (int i = 0; i < TMA_WAIT_LIMIT; ++i) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <bool KICK>
+__global__ void __launch_bounds__(PT) k_gather3_tma(Hot h, const __grid_constant__ CUtensorMap tmap,
+                                                    const int16_t *__restrict__ pmid,
+                                                    const float *__restrict__ disp, float *vel,
+                                                    float *acc, int64_t n,
+                                                    const float *__restrict__ g, float K2,
+                                                    int *err) {
+    extern __shared__ __align__(128) float tbuf[];   // PT/32 boxes, then PT/32 mbarriers
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *box = tbuf + warp * TBOX_PAD;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(tbuf + (PT / 32) * TBOX_PAD) + warp;
+    if (lane == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncwarp();
+    unsigned parity = 0;
+    bool tma_ok = true;   // false after a wait gave up: the warp then reads global memory
+    for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); q0 < n;
+         q0 += (int64_t)gridDim.x * blockDim.x) {   // warp-uniform
+        const int64_t q = q0 + lane;
+        const bool act = q < n;
+        Axis ax[3];
+        if (act) hot_enmesh(h, pmid, q, ld3(disp, q), ax);
+        // the warp's box: unwrapped lower-neighbour indices, z origin on 16 bytes
+        const int x0 = warp_min(act ? ax[0].u : INT_MAX), y0 = warp_min(act ? ax[1].u : INT_MAX);
+        const int z0 = warp_min(act ? ax[2].u : INT_MAX) & ~3;
+        const int x1 = warp_max(act ? ax[0].u : INT_MIN) + 2;
+        const int y1 = warp_max(act ? ax[1].u : INT_MIN) + 2;
+        const int z1 = warp_max(act ? ax[2].u : INT_MIN) + 2;
+        const bool fits = tma_ok && x0 >= 0 && y0 >= 0 && z0 >= 0 && x1 - x0 <= TBX &&
+                          y1 - y0 <= TBY && z1 - z0 <= TBZ && x1 <= h.wrap[0] &&
+                          y1 <= h.wrap[1] && z1 <= h.wrap[2];
+        bool staged = false;
+        if (fits) {   // warp-uniform
+            if (lane == 0) {
+                const unsigned b = smem_addr(bar);
+                // the box's earlier reads (generic proxy) before the copy's writes
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b),
+                             "r"((unsigned)(TBOX * 4))
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                    " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(smem_addr(box)),
+                    "l"(&tmap), "r"(z0), "r"(y0), "r"(0), "r"(x0), "r"(b)
+                    : "memory");
+            }
+            staged = __all_sync(0xffffffffu, mbar_wait(bar, parity));
+            parity ^= 1u;
+            if (!staged) {   // record, wait once more for the copy in flight, then go direct
+                if (lane == 0) atomicExch(err, 1);
+                mbar_wait(bar, parity ^ 1u);
+                tma_ok = false;
+            }
+        }
+        if (act) {
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const float f = frac_of(ax, k);
+                float m0, m1, m2;
+                if (staged) {
+                    const int xi = ax[0].u + (k & 1) - x0, yi = ax[1].u + ((k >> 1) & 1) - y0;
+                    const int zi = ax[2].u + ((k >> 2) & 1) - z0;
+                    const float *b = box + ((xi * 3) * TBY + yi) * TBZ + zi;
+                    m0 = b[0];
+                    m1 = b[TBY * TBZ];
+                    m2 = b[2 * TBY * TBZ];
+                } else {
+                    const float *gc = g + hot_cell(h, ax, k) + (int64_t)ax[0].i[k & 1] * h.gxs;
+                    m0 = __ldg(gc);
+                    m1 = __ldg(gc + h.gjs);
+                    m2 = __ldg(gc + 2 * h.gjs);
+                }
+                a0 = __fadd_rn(a0, __fmul_rn(m0, f));
+                a1 = __fadd_rn(a1, __fmul_rn(m1, f));
+                a2 = __fadd_rn(a2, __fmul_rn(m2, f));
+            }
+            float3 a = make_float3(a0, a1, a2);
+            st3(acc, q, a);
+            if (KICK) st3(vel, q, axpy3(ld3(vel, q), a, K2));
+        }
+        __syncwarp();   // every lane's reads of the box are done before it is refilled
+    }
 }
 
 // Forward: gather the three acceleration meshes, optionally kick with K2.
@@ -1673,6 +1804,7 @@ void ws_free(pmx_workspace *ws) {
     cudaFree(ws->mcot);
     cudaFree(ws->ktab);
     cudaFree(ws->part);
+    cudaFree(ws->err);
     cudaFree(ws->fft_work);
     for (auto &r : ws->recs) {
         cudaEventDestroy(r.b);
@@ -1688,6 +1820,37 @@ size_t buffers_bytes(const int64_t s[3], int32_t flags, int32_t slots) {
     if (flags & PMX_WS_ADJOINT) b += (size_t)M * 4 * 3;
     b += (size_t)NSLOT * PMAX * 8;
     return b * (size_t)slots + (size_t)2 * (s[0] + s[1] + s[2] / 2 + 1) * 4;
+}
+
+// The tensor map of the plane-interleaved acceleration meshes g, (x, 3, n1,
+// n2) float32, for k_gather3_tma's (TBX, 3, TBY, TBZ) boxes.  The encoder is
+// a driver entry point, looked up through the runtime.
+int encode_gather_map(pmx_workspace *ws) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static std::mutex mu;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!encode) {
+            cudaDriverEntryPointQueryResult q;
+            void *fn = nullptr;
+            cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                             cudaEnableDefault, &q);
+            if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+                return fail(PMX_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        }
+    }
+    if (ws->n2 % 4) return fail(PMX_ERR_SHAPE, "TMA gathers need n2 % 4 == 0");
+    const cuuint64_t dims[4] = {(cuuint64_t)ws->n2, (cuuint64_t)ws->n1, 3, (cuuint64_t)ws->n0};
+    const cuuint64_t strides[3] = {(cuuint64_t)ws->n2 * 4, (cuuint64_t)(ws->n1 * ws->n2) * 4,
+                                   (cuuint64_t)(3 * ws->n1 * ws->n2) * 4};
+    const cuuint32_t box[4] = {TBZ, TBY, 3, TBX};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = encode(&ws->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, ws->g, dims, strides, box,
+                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(PMX_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    return PMX_OK;
 }
 
 int check_shape(const int64_t s[3]) {
@@ -1851,6 +2014,21 @@ static int ws_create(const int64_t mesh_shape[3], int32_t flags, int32_t slots,
         ph[0] = &ws->r2c1; ph[1] = &ws->c2r3; ph[2] = &ws->r2c3; ph[3] = &ws->c2r1;
         hv[0] = &ws->have_r2c1; hv[1] = &ws->have_c2r3; hv[2] = &ws->have_r2c3; hv[3] = &ws->have_c2r1;
     }
+    if ((flags & PMX_WS_TMA) && ws->xfast && slots == 1) {
+        if ((st = alloc((void **)&ws->err, sizeof(int)))) { ws_free(ws); return st; }
+        if (cudaMemset(ws->err, 0, sizeof(int)) != cudaSuccess) {
+            ws_free(ws);
+            return fail(PMX_ERR_CUDA, "error word reset failed");
+        }
+        if ((st = encode_gather_map(ws))) { ws_free(ws); return st; }
+        cudaError_t e = cudaFuncSetAttribute(k_gather3_tma<true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TMA_SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_gather3_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)TMA_SMEM);
+        if (e != cudaSuccess) { ws_free(ws); return cuda_status(e, "cudaFuncSetAttribute(k_gather3_tma)"); }
+        ws->tma = true;
+    }
     size_t wmax = 0;
     for (int i = 0; i < 4; ++i)
         if (wk[i] > wmax) wmax = wk[i];
@@ -1912,6 +2090,10 @@ extern "C" int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec, const i
     if (n > 0) {
         {
             Stage sg(ws, 5, s, 1);
+            if (ws->tma)
+                k_gather3_tma<false><<<stride_grid(n, PT), PT, TMA_SMEM, s>>>(
+                    h, ws->tmap, pmid, disp, nullptr, acc, n, ws->g, 0.f, ws->err);
+            else
             k_gather3<false, false><<<stride_grid(n, PT), PT, 0, s>>>(h, pmid, disp, nullptr, acc, n,
                                                                      ws->M, ws->g, 0.f);
             PMX_LAUNCH_CHECK("k_gather3");
@@ -2110,6 +2292,9 @@ static int nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int1
             if (h.vcomp)
                 k_gather3<true, true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, ws->M, ws->g,
                                                        factors[2]);
+            else if (ws->tma)
+                k_gather3_tma<true><<<G, PT, TMA_SMEM, s>>>(h, ws->tmap, pmid, disp, vel, acc, n,
+                                                            ws->g, factors[2], ws->err);
             else
                 k_gather3<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, ws->M, ws->g,
                                                         factors[2]);
@@ -2283,7 +2468,12 @@ static int nbody_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int
             PMX_LAUNCH_CHECK("k_gk_kds");
         } else {
             Stage sg(ws, 5, s, 1);
-            k_gather3<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, ws->M, ws->g, f[2]);
+            if (ws->tma)
+                k_gather3_tma<true><<<G, PT, TMA_SMEM, s>>>(h, ws->tmap, pmid, disp, vel, acc, n,
+                                                            ws->g, f[2], ws->err);
+            else
+                k_gather3<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, n, ws->M, ws->g,
+                                                        f[2]);
             PMX_LAUNCH_CHECK("k_gather3");
         }
     }
@@ -2611,6 +2801,16 @@ extern "C" int pmx_nbody_adj_steps_batch(pmx_workspace *ws, const pmx_enmesh_spe
             PMX_LAUNCH_CHECK("k_sadj_b");
         }
     }
+    return PMX_OK;
+}
+
+extern "C" int pmx_workspace_tma_status(pmx_workspace *ws, int32_t *gave_up) {
+    if (!ws || !gave_up) return fail(PMX_ERR_ARG, "null argument");
+    *gave_up = 0;
+    if (!ws->err) return PMX_OK;
+    int v = 0;
+    PMX_CUDA(cudaMemcpy(&v, ws->err, sizeof(int), cudaMemcpyDeviceToHost));
+    *gave_up = v;
     return PMX_OK;
 }
 

@@ -80,17 +80,27 @@ def test_c2_gradients_vs_central_differences(cuda):
             return float(c2_objective(mm, torch.tensor(om, dtype=torch.float64),
                                       torch.tensor(a_s, dtype=torch.float64), conf))
 
+    def central(fn, h):
+        """Central difference at step h, Richardson-extrapolated with h/2:
+        (4 D(h/2) - D(h)) / 3 cancels the h^2 truncation term, which at the
+        relative step 1e-3 through 63 nonlinear steps reaches the percent
+        level (the step itself is the one the benchmark target asks for)."""
+        d1 = (fn(h) - fn(-h)) / (2 * h)
+        d2 = (fn(h / 2) - fn(-h / 2)) / h
+        return (4 * d2 - d1) / 3, d1
+
     h = 1e-3 * 0.3
-    fd_om = (f(om=0.3 + h) - f(om=0.3 - h)) / (2 * h)
-    assert abs(g_Om / fd_om - 1) < 2e-2, ('Om', g_Om, fd_om)
+    fd_om, fd_om1 = central(lambda e: f(om=0.3 + e), h)
+    assert abs(g_Om / fd_om - 1) < 2e-2, ('Om', g_Om, fd_om, fd_om1)
     h = 1e-3 * 2.1
-    fd_as = (f(a_s=2.1 + h) - f(a_s=2.1 - h)) / (2 * h)
-    assert abs(g_As / fd_as - 1) < 2e-2, ('As', g_As, fd_as)
+    fd_as, fd_as1 = central(lambda e: f(a_s=2.1 + e), h)
+    assert abs(g_As / fd_as - 1) < 2e-2, ('As', g_As, fd_as, fd_as1)
     u = torch.randn(modes.shape, device=cuda, generator=torch.Generator(device=cuda).manual_seed(1))
     u = u / u.norm()
     h = 1e-3 * float(modes.norm())
-    fd_u = (f(h * u) - f(-h * u)) / (2 * h)
+    fd_u, fd_u1 = central(lambda e: f(e * u), h)
     ad = float((g_m * u).sum())
-    print(f'C2: adjoint / central difference - 1: Om {g_Om / fd_om - 1:.2e}, '
-          f'As {g_As / fd_as - 1:.2e}, modes {ad / fd_u - 1:.2e}')
-    assert abs(ad / fd_u - 1) < 2e-2, ('modes', ad, fd_u)
+    print(f'C2: adjoint / central difference - 1: Om {g_Om / fd_om - 1:.2e} '
+          f'(plain {g_Om / fd_om1 - 1:.2e}), As {g_As / fd_as - 1:.2e} '
+          f'(plain {g_As / fd_as1 - 1:.2e}), modes {ad / fd_u - 1:.2e} (plain {ad / fd_u1 - 1:.2e})')
+    assert abs(ad / fd_u - 1) < 2e-2, ('modes', ad, fd_u, fd_u1)

@@ -39,8 +39,6 @@ def _draw(entry, seed, n, layout, cuda):
 @pytest.mark.parametrize('layout', ['original', 'partitionable'])
 @pytest.mark.parametrize('seed, n', [(0, 1), (0, 10), (1, 7), ((5 << 32) + 9, 1001),
                                      (-3, 1 << 20), (12345, (1 << 20) + 3)])
-
-
 def test_bits_and_normals_match_oracle(cuda, layout, seed, n):
     bits = _draw('pmx_random_bits', seed, n, layout, cuda).view(np.uint32)
     np.testing.assert_array_equal(bits, prng.random_bits(prng.prng_key(seed), n, layout))
