@@ -56,6 +56,8 @@ def parse():
     ap.add_argument('--deposit', default='atomic', choices=['atomic', 'agg', 'window'],
                     help='CIC deposits: one float32 reduction per contribution, warp-aggregated '
                          'for particles sharing a cell, or per-warp shared-memory windows')
+    ap.add_argument('--tma', action='store_true',
+                    help='TMA-staged forward gathers (PMX_WS_TMA)')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-full-run', action='store_true',
@@ -269,7 +271,7 @@ def workload_config(args, world):
                         f'K forward leapfrog steps then their K reversible-adjoint steps of a '
                         f'{args.nbody_steps}-step run (rates per fwd+adj step pair)',
             'ptcl': side ** 3, 'mesh_cells': mside ** 3, 'parallelism': f'replicas x{world}',
-            'deposit': args.deposit,
+            'deposit': args.deposit, 'tma_gathers': bool(args.tma),
             'l2': 'inputs larger than L2 (mesh 4.3 GB per array)'}
 
 
@@ -353,7 +355,7 @@ def run_pmx(args, rank, world, local_rank):
     Om = float(cosmo.Omega_m)
 
     ws = _lib.Workspace(conf.mesh_shape, adjoint=True, agg=args.deposit == 'agg',
-                        window=args.deposit == 'window')
+                        window=args.deposit == 'window', tma=args.tma)
     spec = _lib.make_spec(3, conf.mesh_shape, conf.mesh_shape, conf.cell_size)
     dots = torch.zeros(4, dtype=torch.float64, device=dev)
     P = _lib.ptr

@@ -134,18 +134,20 @@ typedef struct pmx_workspace pmx_workspace;
                               directly instead of replaying captured graphs */
 #define PMX_WS_PLANE16 64  /* plane kernels in clusters of 16 CTAs (the
                               non-portable size) instead of 8 */
-#define PMX_WS_TMA 256     /* forward gathers stage each warp's box of the
-                              acceleration meshes in shared memory with one
-                              cp.async.bulk.tensor copy (fused x-pass path,
-                              n2 % 4 == 0, single-simulation workspaces) */
 #define PMX_WS_AGG 128     /* warp-aggregated deposits: lanes whose particles
                               share a cell sum their contributions in shared
                               memory and one lane issues the reductions
                               (helps clustered late-time states) */
+#define PMX_WS_TMA 65536   /* forward gathers stage each warp's box of the
+                              acceleration meshes in shared memory with one
+                              cp.async.bulk.tensor copy (fused x-pass path,
+                              n2 % 4 == 0, single-simulation workspaces;
+                              opt-in: slower than the global-load gathers on
+                              GB300) */
 /* Slab-wise plane transforms: number of concurrent chains (1..4; 0 = the
- * default 2) and log2 of the x-planes per cuFFT execution (1..15; 0 = the
- * default, the smallest power of two >= 8 reaching 32 MB), packed into the
- * flags.  Results do not depend on either. */
+ * default 2) in bits 8..10 and log2 of the x-planes per cuFFT execution
+ * (1..15; 0 = the default, the smallest power of two >= 8 reaching 32 MB) in
+ * bits 12..15 of the flags.  Results do not depend on either. */
 #define PMX_WS_CHAINS_SHIFT 8
 #define PMX_WS_SLAB_SHIFT 12
 #define PMX_WS_CHAINS(k) (((k) & 7) << PMX_WS_CHAINS_SHIFT)

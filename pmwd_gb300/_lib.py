@@ -117,7 +117,7 @@ PMX_WS_VEC = 16
 PMX_WS_NO_GRAPH = 32
 PMX_WS_PLANE16 = 64
 PMX_WS_AGG = 128
-PMX_WS_TMA = 256
+PMX_WS_TMA = 1 << 16
 PMX_WS_CHAINS_SHIFT = 8
 PMX_WS_SLAB_SHIFT = 12
 

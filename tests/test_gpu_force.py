@@ -477,12 +477,19 @@ def test_aggregated_deposits_equal_direct_atomics(cuda, state):
     assert abs(o1 / o2 - 1) < 1e-4
     # 4 forward steps, then 4 reverse steps (which amplify the order noise)
     assert rel_l2(x1, x2) < 1e-5 and rel_l2(y1, y2) < 1e-4
-    # the adjoint's vel_cot: in dense clumps a rounding-level change of a
-    # reconstructed position moves many particles across cell boundaries,
-    # where the CIC weight gradient jumps; two runs of the direct path
-    # differ as much, so the bound is ten times their difference
-    floor = rel_l2(v3, v2)
-    assert rel_l2(v1, v2) < max(1e-3, 10 * floor), (rel_l2(v1, v2), floor)
+    # the adjoint's vel_cot: a rounding-level change of a reconstructed
+    # position (here: another summation order of the deposits) can move a
+    # particle across a cell boundary, where the CIC weight gradient jumps
+    # and its cotangent changes by O(1).  As in the multi-step test, 0.2% of
+    # the particles are set aside; the rest are held to ten times the
+    # difference between two runs of the direct path (at least 1e-3), and
+    # the whole array to 3e-2 or ten times that difference.
+    def kept(a, b):
+        e = np.linalg.norm(a - b, axis=1)
+        keep = np.argsort(e)[:len(e) - len(e) // 500]
+        return rel_l2(a[keep], b[keep])
+    assert kept(v1, v2) < max(1e-3, 10 * kept(v3, v2)), (kept(v1, v2), kept(v3, v2))
+    assert rel_l2(v1, v2) < max(3e-2, 10 * rel_l2(v3, v2)), (rel_l2(v1, v2), rel_l2(v3, v2))
 
 
 @pytest.mark.parametrize('case', ['near_lattice', 'scattered'])
