@@ -494,6 +494,9 @@ def run_pmx(args, rank, world, local_rank):
     dom = max(own, key=lambda k: own[k]['ms_per_step'])
     ach = stage_rows[dom]['gbs']
     tr = traffic.get(dom)
+    # the summary is of the 512^3 / 1024^3 step; every operand scales with
+    # N (M = 8 N at mesh factor 2), other mesh factors have no capture
+    tr = tr * N / 512 ** 3 if tr is not None and args.mesh == 2 else None
     roofline = {'bound': 'hbm', 'kernel': dom, 'achieved': ach, 'peak': peak, 'unit': 'GB/s',
                 'frac': ach / peak, 'traffic': tr,
                 'algorithmic_bytes': ab[dom], 'peak_kind': f'{peak_kind} (MEASURED_PEAKS.json hbm_gbs)'

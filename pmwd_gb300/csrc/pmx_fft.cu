@@ -209,6 +209,7 @@ struct XCfg {
     static constexpr int CS = pad_cs(N, R2, T);
     static constexpr int BUF = T * CS;  // float2 per buffer
     static constexpr int PER = N * T / XTH;  // tile elements per thread
+    static constexpr int TWP = R1 * (R2 + 1);  // padded twiddle table entries
     __device__ static __forceinline__ int at(int t, int p) { return t * CS + p + p / R2; }
 };
 
@@ -226,10 +227,23 @@ __device__ __forceinline__ void cp_async_wait_group1() {
     asm volatile("cp.async.wait_group 1;\n" ::: "memory");
 }
 
+// Twiddles w^(b k1) (w = exp(-2 pi i / n0), b < R2, k1 < R1) in a padded
+// table twP[k1 (R2 + 1) + b]: step 1 reads it with the lanes on b
+// (consecutive entries), the inverse step 2 with the lanes on k1 (an odd
+// stride of 8-byte entries), so neither has shared-memory bank conflicts.
+// A flat table read at b k1 has power-of-two strides in both.
+template <class C>
+__device__ __forceinline__ void fill_twiddles(const float2 *__restrict__ twg, float2 *twP) {
+    for (int m = threadIdx.x; m < C::R1 * (C::R2 + 1); m += C::TH) {
+        const int k1 = m / (C::R2 + 1), b = m % (C::R2 + 1);
+        twP[m] = b < C::R2 ? twg[b * k1] : make_float2(0.f, 0.f);
+    }
+}
+
 // Forward step 1 on one buffer: R2-strided radix-R1 DFTs + twiddles,
 // natural order -> "transposed" positions k1*R2 + b.
 template <class C>
-__device__ __forceinline__ void fwd_step1(float2 *buf, const float2 *tw) {
+__device__ __forceinline__ void fwd_step1(float2 *buf, const float2 *twP) {
     constexpr int R1 = C::R1, R2 = C::R2;
     for (int it = threadIdx.x; it < C::T * R2; it += C::TH) {
         const int t = it / R2, b = it % R2;
@@ -241,7 +255,7 @@ __device__ __forceinline__ void fwd_step1(float2 *buf, const float2 *tw) {
 #pragma unroll
         for (int k = 0; k < R1; ++k) {
             const int k1 = brev(k, Log2<R1>::v);
-            col[k1 * (R2 + 1)] = cmul(v[k], tw[b * k1]);
+            col[k1 * (R2 + 1)] = cmul(v[k], twP[k1 * (R2 + 1) + b]);
         }
     }
 }
@@ -267,7 +281,7 @@ __device__ __forceinline__ void inv_step1(float2 *buf) {
 // forward step 2 leaves it), twiddle, store to positions k1*R2 + b.
 template <class C>
 __device__ __forceinline__ void inv_step2_store(float2 (&v)[C::R2], float2 *buf, int t, int k1,
-                                                const float2 *tw) {
+                                                const float2 *twP) {
     constexpr int R2 = C::R2;
     float2 u[R2];
     unbrev<R2>(v, u);           // natural k2 order
@@ -276,7 +290,7 @@ __device__ __forceinline__ void inv_step2_store(float2 (&v)[C::R2], float2 *buf,
 #pragma unroll
     for (int k = 0; k < R2; ++k) {
         const int b = brev(k, Log2<R2>::v);
-        grp[b] = cmulc(u[k], tw[b * k1]);
+        grp[b] = cmulc(u[k], twP[k1 * (R2 + 1) + b]);
     }
 }
 
@@ -332,14 +346,14 @@ __global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__
     constexpr int T = C::T, R1 = C::R1, R2 = C::R2;
     extern __shared__ __align__(16) float2 smem2[];
     float2 *A0 = smem2, *A1 = smem2 + C::BUF, *B = smem2 + 2 * C::BUF;
-    float2 *tw = smem2 + 3 * C::BUF;
-    float *kxs = reinterpret_cast<float *>(tw + N), *mxs = kxs + N;
+    float2 *twP = smem2 + 3 * C::BUF;
+    float *kxs = reinterpret_cast<float *>(twP + C::TWP), *mxs = kxs + N;
 
     const int64_t tot = n0 + g.n1 + g.n2h;
     const float *ky = kt + n0, *kz = kt + n0 + g.n1;
     const float *my = kt + tot + n0, *mz = kt + tot + n0 + g.n1;
+    fill_twiddles<C>(twg, twP);
     for (int m = threadIdx.x; m < N; m += XTF) {
-        tw[m] = twg[m];
         kxs[m] = kt[m];
         mxs[m] = kt[tot + m];
     }
@@ -359,7 +373,7 @@ __global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__
         const int64_t nxt = tile + gridDim.x;
         if (nxt < ntiles) issue_tile<C>(H, 1, 0, g.row(nxt), g.col0(nxt, T), g, cur ? A0 : A1);
         cp_async_commit();
-        fwd_step1<C>(A, tw);
+        fwd_step1<C>(A, twP);
         __syncthreads();
         // fused: forward step 2, Green + gradient, inverse step 2 of P and of
         // B = -i kx P, all on one thread's contiguous group
@@ -386,8 +400,8 @@ __global__ void __launch_bounds__(XTF, 1) k_xpass_fwd(const float2 *__restrict__
                 v[k] = make_float2(pr, pi);
                 w[k] = make_float2(__fmul_rn(mxi, pi), -__fmul_rn(mxi, pr));  // -i kx P
             }
-            inv_step2_store<C>(v, A, t, k1, tw);
-            inv_step2_store<C>(w, B, t, k1, tw);
+            inv_step2_store<C>(v, A, t, k1, twP);
+            inv_step2_store<C>(w, B, t, k1, twP);
         }
         __syncthreads();
         inv_step1<C>(A);
@@ -456,14 +470,14 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
     constexpr int T = C::T, R1 = C::R1, R2 = C::R2;
     extern __shared__ __align__(16) float2 smem2[];
     float2 *A0 = smem2, *A1 = smem2 + C::BUF, *B = smem2 + 2 * C::BUF;
-    float2 *tw = smem2 + 3 * C::BUF;
-    float *kxs = reinterpret_cast<float *>(tw + N), *mxs = kxs + N;
+    float2 *twP = smem2 + 3 * C::BUF;
+    float *kxs = reinterpret_cast<float *>(twP + C::TWP), *mxs = kxs + N;
 
     const int64_t tot = n0 + g.n1 + g.n2h;
     const float *ky = kt + n0, *kz = kt + n0 + g.n1;
     const float *my = kt + tot + n0, *mz = kt + tot + n0 + g.n1;
+    fill_twiddles<C>(twg, twP);
     for (int m = threadIdx.x; m < N; m += XTA) {
-        tw[m] = twg[m];
         kxs[m] = kt[m];
         mxs[m] = kt[tot + m];
     }
@@ -485,8 +499,8 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
         load_comb<C>(Cin, j, l0, myj, mz, g, B);
         cp_async_wait_group1();  // this tile's C_0 (the next tile's may stay in flight)
         __syncthreads();
-        fwd_step1<C>(A, tw);
-        fwd_step1<C>(B, tw);
+        fwd_step1<C>(A, twP);
+        fwd_step1<C>(B, twP);
         __syncthreads();
         const float kyj = __ldg(ky + j);
         const float ky2 = __fmul_rn(kyj, kyj);
@@ -512,7 +526,7 @@ __global__ void __launch_bounds__(XTA, 1) k_xpass_adj(const float2 *__restrict__
                 const float rk = k2v != 0.f ? __fdividef(g.c, k2v) : 0.f;
                 v[k] = make_float2(-__fmul_rn(re, rk), -__fmul_rn(im, rk));
             }
-            inv_step2_store<C>(v, A, t, k1, tw);
+            inv_step2_store<C>(v, A, t, k1, twP);
         }
         __syncthreads();
         inv_step1<C>(A);
@@ -535,7 +549,7 @@ template <int N>
 size_t xpass_smem(bool adj) {
     using CF = XCfg<N, XTF>;
     using CA = XCfg<N, XTA>;
-    const size_t tables = (size_t)N * (sizeof(float2) + 2 * sizeof(float));
+    const size_t tables = (size_t)CF::TWP * sizeof(float2) + (size_t)N * 2 * sizeof(float);
     return (size_t)3 * (adj ? CA::BUF : CF::BUF) * sizeof(float2) + tables;
 }
 
