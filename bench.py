@@ -378,12 +378,18 @@ def run_pmx(args, rank, world, local_rank):
                                            sa.ctypes.data_as(ctypes.c_void_p), Om,
                                            P(seg_dots), stream), 'pmx_nbody_adj_steps')
 
-    def step(stream):
+    def step_fwd(stream):
         _lib.check(lib.pmx_nbody_step(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc), N, N,
                                       f_fwd, Om, stream), 'pmx_nbody_step')
+
+    def step_adj(stream):
         _lib.check(lib.pmx_nbody_adj_step(ws.handle, spec, P(pmid), P(disp), P(vel), P(acc),
                                           P(disp_cot), P(vel_cot), P(alpha), N, N, f_adj, Om,
                                           P(dots), stream), 'pmx_nbody_adj_step')
+
+    def step(stream):
+        step_fwd(stream)
+        step_adj(stream)
 
     stream = torch.cuda.current_stream(dev)
     sp = _lib.c_p(stream.cuda_stream)
@@ -433,31 +439,59 @@ def run_pmx(args, rank, world, local_rank):
         outs = ('disp', 'vel', 'acc', 'disp_cot', 'vel_cot', 'alpha')
         d2h = sum(host[k].numel() * host[k].element_size() for k in outs)
         ke = max(2, min(args.steps, 5))
-        # one copy stream per buffer: copies of different buffers overlap,
-        # and a buffer's read-back overlaps other buffers' uploads; each
-        # buffer's copies stay in order on its own stream
-        cstreams = {k: torch.cuda.Stream(dev) for k in host}
+        # Each step's inputs are the previous step's results read back to
+        # the host.  One stream uploads and one downloads, each in order
+        # (a GB300's link to its Grace host carries both directions at once:
+        # 211 GB/s up and 194 GB/s down, 343 GB/s together, measured; many
+        # copy streams of mixed directions got 203 GB/s in all).  A
+        # buffer goes up once the previous step no longer reads its device
+        # copy and its download has landed; the forward step starts once
+        # its own inputs are up, while the adjoint's inputs still upload.
+        # Copies go in chunks of 256 MB, so an upload trails the download of
+        # the same buffer by one chunk instead of one buffer.
+        fwd_in = ('pmid', 'disp', 'vel', 'acc')
+        adj_in = ('disp_cot', 'vel_cot', 'alpha')
+        chunk = 256 << 20
+
+        def pieces(k):
+            d, h = dev_bufs[k].view(-1), host[k].view(-1)
+            step_n = max(1, chunk // d.element_size())
+            return [(d[a:a + step_n], h[a:a + step_n]) for a in range(0, d.numel(), step_n)]
+
+        parts = {k: pieces(k) for k in host}
+        up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
         barrier()
         e0.record(stream)
-        done = None
+        up.wait_stream(stream)
+        done, landed = None, {}
         for _ in range(ke):
-            for k, v in host.items():
-                s = cstreams[k]
-                if done is not None:
-                    s.wait_event(done)      # the previous step no longer reads it
-                with torch.cuda.stream(s):
-                    dev_bufs[k].copy_(v, non_blocking=True)
-                stream.wait_stream(s)
-            step(sp)
+            if done is not None:
+                up.wait_event(done)           # the previous step no longer reads them
+            marks = {}
+            for k in fwd_in + adj_in:
+                for c, (d, h) in enumerate(parts[k]):
+                    if (k, c) in landed:
+                        up.wait_event(landed[k, c])   # the previous result is on the host
+                    with torch.cuda.stream(up):
+                        d.copy_(h, non_blocking=True)
+                if k in ('acc', 'alpha'):
+                    marks[k] = torch.cuda.Event()
+                    marks[k].record(up)
+            stream.wait_event(marks['acc'])
+            step_fwd(sp)
+            stream.wait_event(marks['alpha'])
+            step_adj(sp)
             done = torch.cuda.Event()
             done.record(stream)
+            down.wait_event(done)
             for k in outs:
-                s = cstreams[k]
-                s.wait_event(done)
-                with torch.cuda.stream(s):
-                    host[k].copy_(dev_bufs[k], non_blocking=True)
-        for s in cstreams.values():
-            stream.wait_stream(s)
+                for c, (d, h) in enumerate(parts[k]):
+                    with torch.cuda.stream(down):
+                        h.copy_(d, non_blocking=True)
+                    landed[k, c] = torch.cuda.Event()
+                    landed[k, c].record(down)
+        stream.wait_stream(down)
+        stream.wait_stream(up)
         e1.record(stream)
         barrier()
         t = torch.tensor([e0.elapsed_time(e1)], dtype=torch.float64, device=dev)
@@ -466,8 +500,10 @@ def run_pmx(args, rank, world, local_rank):
         e2e = {'value': world * N * ke / (float(t) / 1e3), 'unit': UNIT,
                'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
                'steps': ke, 'path': 'pmx_nbody_step + pmx_nbody_adj_step (C ABI), pinned host '
-                                    'buffers copied in and out every step (one copy stream '
-                                    'per buffer)'}
+                                    'buffers copied in and out every step, each step\'s inputs '
+                                    'the previous step\'s results read back (one upload and one '
+                                    'download stream, 256 MB chunks; the adjoint inputs upload '
+                                    'during the forward step)'}
 
     # ---- the whole run: every forward step, then every adjoint step ----
     full = None
