@@ -460,6 +460,32 @@ def run_pmx(args, rank, world, local_rank):
 
         parts = {k: pieces(k) for k in host}
         up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+        def link_rate():
+            """This machine's host link for one 1.6 GB buffer: up, down, both at
+            once (GB/s), for reading the e2e figure."""
+            d, h = dev_bufs['disp'], host['disp']
+            d2, h2 = dev_bufs['vel'], host['vel']
+            nb = d.numel() * d.element_size()
+            out = {}
+            for name, jobs in (('h2d', [(up, d, h)]), ('d2h', [(down, h, d)]),
+                               ('both', [(up, d, h), (down, h2, d2)])):
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                for st_, dst, src in jobs:
+                    st_.wait_stream(stream)
+                    with torch.cuda.stream(st_):
+                        dst.copy_(src, non_blocking=True)
+                    stream.wait_stream(st_)
+                b.record(stream)
+                torch.cuda.synchronize()
+                out[name] = len(jobs) * nb / (a.elapsed_time(b) / 1e3) / 1e9
+            for k in ('disp', 'vel'):       # the buffers hold the step state again
+                host[k].copy_(dev_bufs[k])
+            return out
+
+        link = link_rate()
         barrier()
         e0.record(stream)
         up.wait_stream(stream)
@@ -499,7 +525,7 @@ def run_pmx(args, rank, world, local_rank):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e = {'value': world * N * ke / (float(t) / 1e3), 'unit': UNIT,
                'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
-               'steps': ke, 'path': 'pmx_nbody_step + pmx_nbody_adj_step (C ABI), pinned host '
+               'steps': ke, 'link_gbs': link, 'path': 'pmx_nbody_step + pmx_nbody_adj_step (C ABI), pinned host '
                                     'buffers copied in and out every step, each step\'s inputs '
                                     'the previous step\'s results read back (one upload and one '
                                     'download stream, 256 MB chunks; the adjoint inputs upload '

@@ -213,13 +213,15 @@ def test_results_same_alone_and_in_mix(cuda):
     mixed, st_mix = srv.run(reqs, realtime=False)
     srv.close()
     assert st_mix['sims'] == len(reqs) == st_seq['sims']
+    # gradients: the bound of the batched-group test below, for the same
+    # reason (atomic order, CIC cell boundaries)
     for a, m in zip(alone, mixed):
         assert a.rid == m.rid
         assert abs(m.obj / a.obj - 1) < 1e-4, (a, m)
         assert abs(m.disp_rms / a.disp_rms - 1) < 1e-5
         if a.grad_rms is not None:
-            assert abs(m.grad_rms / a.grad_rms - 1) < 1e-3
-            assert abs(m.dobj_dOm / a.dobj_dOm - 1) < 1e-3
+            assert abs(m.grad_rms / a.grad_rms - 1) < 5e-3
+            assert abs(m.dobj_dOm / a.dobj_dOm - 1) < 5e-3
 
 
 @pytest.mark.gpu
@@ -237,13 +239,15 @@ def test_results_same_alone_and_in_one_batched_group(cuda):
     mixed, st = srv.run(reqs, realtime=False)
     srv.close()
     assert st['sims'] == 5 and st['failed'] == 0
-    # d obj / d Omega_m sums the force sensitivity over every step: the order
-    # of the float32 atomic adds moves a reconstructed particle across a CIC
-    # cell boundary now and then, where the weight gradient jumps (measured
-    # 1.9e-3 between the batched and the single-simulation run)
+    # the gradients sum cotangents over every step: the order of the float32
+    # atomic adds moves a reconstructed particle across a CIC cell boundary
+    # now and then, where the weight gradient jumps, and with 32^3 particles
+    # one such particle moves the modes gradient's rms by a few 1e-3
+    # (measured between the batched and the single-simulation run: 1.9e-3
+    # for d obj / d Omega_m, 2.5e-3 for the rms)
     for a, m in zip(alone, mixed):
         assert abs(m.obj / a.obj - 1) < 1e-4, (a, m)
         assert abs(m.disp_rms / a.disp_rms - 1) < 1e-5
         if a.grad_rms is not None:
-            assert abs(m.grad_rms / a.grad_rms - 1) < 1e-3
+            assert abs(m.grad_rms / a.grad_rms - 1) < 5e-3
             assert abs(m.dobj_dOm / a.dobj_dOm - 1) < 5e-3
