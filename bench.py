@@ -470,17 +470,21 @@ def run_pmx(args, rank, world, local_rank):
             out = {}
             for name, jobs in (('h2d', [(up, d, h)]), ('d2h', [(down, h, d)]),
                                ('both', [(up, d, h), (down, h2, d2)])):
-                torch.cuda.synchronize()
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                for st_, dst, src in jobs:
-                    st_.wait_stream(stream)
-                    with torch.cuda.stream(st_):
-                        dst.copy_(src, non_blocking=True)
-                    stream.wait_stream(st_)
-                b.record(stream)
-                torch.cuda.synchronize()
-                out[name] = len(jobs) * nb / (a.elapsed_time(b) / 1e3) / 1e9
+                best = 0.0
+                for _ in range(3):           # the first copies warm the engines
+                    torch.cuda.synchronize()
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    for st_, dst, src in jobs:
+                        st_.wait_stream(stream)
+                        with torch.cuda.stream(st_):
+                            dst.copy_(src, non_blocking=True)
+                        stream.wait_stream(st_)
+                    b.record(stream)
+                    torch.cuda.synchronize()
+                    best = max(best, len(jobs) * nb / (a.elapsed_time(b) / 1e3) / 1e9)
+                out[name] = best
             for k in ('disp', 'vel'):       # the buffers hold the step state again
                 host[k].copy_(dev_bufs[k])
             return out
