@@ -33,7 +33,7 @@ using namespace pmx;
 
 namespace {
 
-constexpr int PMAX = 4096;       // max blocks of a particle kernel (partials per slot)
+constexpr int PMAX = 65536;      // max blocks of a particle kernel (partials per slot)
 constexpr int BMAX = 16;         // most simulations of one batched call
 constexpr int NSLOT = 4;         // dot-product slots
 constexpr int PT = 256;          // threads per particle kernel
@@ -1227,16 +1227,18 @@ __global__ void __launch_bounds__(PT) k_sa_ka(Hot h, const int16_t *__restrict__
 
 // Sums the per-block partials in a fixed order: dots[s] = sum of slot s for
 // s < nslots (dots may be NULL), and *om_out = om_scale * sum of slot 2
-// (om_out may be NULL).
-__global__ void k_finish(const double *part, int nblk, double *dots, int nslots, double *om_out,
-                         double om_scale) {
+// (om_out may be NULL).  Slot 2 holds nblk2 partials (the gather VJP's
+// grid), the other slots nblk.
+__global__ void k_finish(const double *part, int nblk, int nblk2, double *dots, int nslots,
+                         double *om_out, double om_scale) {
     __shared__ double sh[32];
     int last = nslots > 3 ? nslots : 3;
     for (int s = 0; s < last; ++s) {
         bool want = (dots && s < nslots) || (om_out && s == 2);
         if (!want) continue;
+        const int nb = s == 2 ? nblk2 : nblk;
         double v = 0.0;
-        for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += part[s * PMAX + b];
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) v += part[s * PMAX + b];
         double t = block_sum<1024>(v, sh);
         if (threadIdx.x == 0) {
             if (dots && s < nslots) dots[s] = t;
@@ -1435,6 +1437,23 @@ __global__ void k_reduce1(const double *part, int nblk, double *out) {
 namespace {
 
 int grid_fill(int64_t n) { return stride_grid((n + 3) / 4, 256, 16); }
+
+// Blocks of a grid-stride particle kernel: up to per_sm per SM, at most
+// PMAX.  Many short blocks beat a few long-running ones.  The block
+// scheduler starts a new block whenever one ends, so warps slowed by
+// contended atomics (the halos of late, clustered steps) hold up only their
+// own block and not a fixed share of the particles.  Measured on a
+// 512^3-particle / 1024^3-mesh run: a 100 + 100 step forward and adjoint
+// run takes 120 ms per step pair at 65536 blocks, 130 at 64 per SM, 140 at
+// 8 per SM; the early steps 90.9 / 91.4 / 93.8 ms; one resident wave of
+// blocks was slower still.
+int ptcl_grid(int64_t n, int per_sm = PMAX) {
+    const int g = stride_grid(n, PT, per_sm);
+    return g > PMAX ? PMAX : g;
+}
+// The joined scatter-VJP / adjoint-kick pass measured best at 64 blocks per
+// SM (5.59 vs 5.84 ms per launch at 65536 blocks).
+constexpr int SAKA_PER_SM = 64;
 
 // Per-device reduction scratch for the stand-alone dot entry points,
 // allocated once at their first use on a device.
@@ -2080,7 +2099,7 @@ extern "C" int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec, const i
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
-            PMX_WIN_LAUNCH(h, k_kds, (false), stride_grid(n, PT), WIN1_SMEM, s,
+            PMX_WIN_LAUNCH(h, k_kds, (false), ptcl_grid(n), WIN1_SMEM, s,
                            (h, pmid, const_cast<float *>(disp), nullptr, nullptr, n, 0.f, 0.f,
                             ws->dens));
             PMX_LAUNCH_CHECK("k_kds");
@@ -2091,11 +2110,11 @@ extern "C" int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec, const i
         {
             Stage sg(ws, 5, s, 1);
             if (ws->tma)
-                k_gather3_tma<false><<<stride_grid(n, PT), PT, TMA_SMEM, s>>>(
+                k_gather3_tma<false><<<ptcl_grid(n), PT, TMA_SMEM, s>>>(
                     h, ws->tmap, pmid, disp, nullptr, acc, n, ws->g, 0.f, ws->err);
             else
-            k_gather3<false, false><<<stride_grid(n, PT), PT, 0, s>>>(h, pmid, disp, nullptr, acc, n,
-                                                                     ws->M, ws->g, 0.f);
+            k_gather3<false, false><<<ptcl_grid(n), PT, 0, s>>>(h, pmid, disp, nullptr, acc, n,
+                                                                ws->M, ws->g, 0.f);
             PMX_LAUNCH_CHECK("k_gather3");
         }
     }
@@ -2119,8 +2138,7 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
         k_fill<<<grid_fill(3 * ws->M), 256, 0, s>>>(ws->mcot, 0.f, 3 * ws->M);
         PMX_LAUNCH_CHECK("k_fill");
     }
-    int G = stride_grid(n, PT);
-    if (G > PMAX) G = PMAX;
+    const int G = ptcl_grid(n);
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
@@ -2161,7 +2179,8 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
         } else {
             {
                 Stage sg(ws, 12, s, 1);
-                k_finish<<<1, 1024, 0, s>>>(ws->part, G, nullptr, 0, omega_m_cot, om_scale(omega_m));
+                k_finish<<<1, 1024, 0, s>>>(ws->part, G, G, nullptr, 0, omega_m_cot,
+                                            om_scale(omega_m));
                 PMX_LAUNCH_CHECK("k_finish");
             }
         }
@@ -2276,7 +2295,7 @@ static int nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int1
         k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
         PMX_LAUNCH_CHECK("k_fill");
     }
-    int G = stride_grid(n, PT);
+    const int G = ptcl_grid(n);
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
@@ -2330,8 +2349,7 @@ static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const 
         PMX_CUDA(cudaMemsetAsync(dots, 0, 4 * sizeof(double), s));
         return PMX_OK;
     }
-    int G = stride_grid(n, PT);
-    if (G > PMAX) G = PMAX;
+    const int G = ptcl_grid(n);
     {
         Stage sg(ws, 6, s, 1);
         PMX_WIN_LAUNCH(h, k_ka, (true), G, WIN1_SMEM, s,
@@ -2366,7 +2384,7 @@ static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const 
     }
     {
         Stage sg(ws, 12, s, 1);
-        k_finish<<<1, 1024, 0, s>>>(ws->part, G, dots, 3, dots + 3, om_scale(omega_m));
+        k_finish<<<1, 1024, 0, s>>>(ws->part, G, G, dots, 3, dots + 3, om_scale(omega_m));
         PMX_LAUNCH_CHECK("k_finish");
     }
     return PMX_OK;
@@ -2434,7 +2452,7 @@ static int nbody_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int
     }
     cudaStream_t s = as_stream(stream);
     if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
-    const int G = stride_grid(n, PT);
+    const int G = ptcl_grid(n);
     {
         Stage sg(ws, 0, s, 1);
         k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
@@ -2503,8 +2521,8 @@ static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const
     }
     cudaStream_t s = as_stream(stream);
     if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
-    int G = stride_grid(n, PT);
-    if (G > PMAX) G = PMAX;
+    const int G = ptcl_grid(n), Gsaka = ptcl_grid(n, SAKA_PER_SM);
+    int nb01 = G;  // blocks of the kernel that last wrote dot slots 0 and 1
     {
         Stage sg(ws, 0, s, 2);
         k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
@@ -2538,7 +2556,7 @@ static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const
         }
         {
             Stage sg(ws, 12, s, 1);
-            k_finish<<<1, 1024, 0, s>>>(ws->part, G, dots + 4 * i, 3, dots + 4 * i + 3,
+            k_finish<<<1, 1024, 0, s>>>(ws->part, nb01, G, dots + 4 * i, 3, dots + 4 * i + 3,
                                         om_scale(omega_m));
             PMX_LAUNCH_CHECK("k_finish");
         }
@@ -2552,13 +2570,15 @@ static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const
             }
             Stage sg(ws, 14, s, 1);
             if (h.agg)
-                k_sa_ka<true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot,
-                                               n, ws->rcot_of(1), f[2], f[3], f[4], ws->dens,
-                                               ws->part);
+                k_sa_ka<true><<<Gsaka, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot,
+                                                   acc_cot, n, ws->rcot_of(1), f[2], f[3], f[4],
+                                                   ws->dens, ws->part);
             else
-                k_sa_ka<<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n,
-                                         ws->rcot_of(1), f[2], f[3], f[4], ws->dens, ws->part);
+                k_sa_ka<<<Gsaka, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot,
+                                             n, ws->rcot_of(1), f[2], f[3], f[4], ws->dens,
+                                             ws->part);
             PMX_LAUNCH_CHECK("k_sa_ka");
+            nb01 = Gsaka;
         } else {
             Stage sg(ws, 11, s, 1);
             k_sadj<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n,
@@ -2641,8 +2661,7 @@ int batch_prepare(pmx_workspace *ws, const pmx_enmesh_spec *spec, int32_t nsim,
         bc->fin.oms[b] = om_scale(q.omega_m);
         if (q.n > nmax) nmax = q.n;
     }
-    int G = stride_grid(nmax, PT);
-    bc->G = G > PMAX ? PMAX : G;
+    bc->G = ptcl_grid(nmax);
     return PMX_OK;
 }
 

@@ -96,10 +96,10 @@ def request_bytes(side, grad):
 
 def workspace_bytes(mesh_side):
     """Meshes and spectra of one workspace slot plus a cuFFT work-area
-    allowance."""
+    allowance and the per-block float64 partial sums (4 x 65536)."""
     m = mesh_side ** 3
     mc = mesh_side * mesh_side * (mesh_side // 2 + 1)
-    return 4 * m + 3 * 8 * mc + 6 * 4 * m + 8 * mc
+    return 4 * m + 3 * 8 * mc + 6 * 4 * m + 8 * mc + 4 * 65536 * 8
 
 
 def batchable(mesh_side):
