@@ -61,6 +61,15 @@ const char *pmx_last_error(void);
 /* Number of SMs of the current device, used to size persistent grids. */
 int pmx_device_sms(int *sms);
 
+/* A non-blocking CUDA stream of the library's own on `device`, and its
+ * release.  No counterpart in the reference (JAX owns its streams).  For
+ * host code whose stream API hands out streams from a fixed pool --
+ * torch.cuda.Stream() draws from 32 per device -- and that captures CUDA
+ * graphs from several threads: a capture on a pooled stream would also
+ * record the work another thread launches on that same stream. */
+int pmx_stream_create(int device, void **stream);
+int pmx_stream_destroy(void *stream);
+
 /* --------------------------------------------------------------------------
  * Mesh operators
  * ------------------------------------------------------------------------ */

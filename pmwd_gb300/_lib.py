@@ -40,6 +40,8 @@ SIGNATURES = {
     'pmx_version': (c_int, []),
     'pmx_last_error': (ctypes.c_char_p, []),
     'pmx_device_sms': (c_int, [ctypes.POINTER(c_int)]),
+    'pmx_stream_create': (c_int, [c_int, ctypes.POINTER(c_p)]),
+    'pmx_stream_destroy': (c_int, [c_p]),
     'pmx_enmesh': (c_int, [ctypes.POINTER(EnmeshSpec), c_p, c_p, c_i64, c_p, c_p, c_p, c_p]),
     'pmx_scatter': (c_int, [ctypes.POINTER(EnmeshSpec), c_p, c_p, c_i64, c_p, c_f, c_i64, c_p, c_p]),
     'pmx_scatter_adj': (c_int, [ctypes.POINTER(EnmeshSpec), c_p, c_p, c_i64, c_p, c_f, c_i64, c_p,
@@ -174,6 +176,29 @@ def ptr(t):
 
 def stream_ptr(device=None):
     return c_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+_OWN_STREAMS = {}
+_OWN_LOCK = threading.Lock()
+
+
+def own_stream(device):
+    """A CUDA stream the library created on ``device`` (one per device, kept
+    for the life of the process), as a ``torch.cuda.ExternalStream``.
+    ``torch.cuda.Stream()`` hands out streams from a fixed pool (32 per
+    device), so a pooled stream may be the one another thread launches its
+    work on; graph captures use this stream instead, so that a capture
+    never records another thread's work."""
+    dev = torch.device(device)
+    idx = dev.index if dev.index is not None else torch.cuda.current_device()
+    with _OWN_LOCK:
+        s = _OWN_STREAMS.get(idx)
+        if s is None:
+            h = c_p()
+            check(load().pmx_stream_create(idx, ctypes.byref(h)), 'pmx_stream_create')
+            s = torch.cuda.ExternalStream(h.value, device=torch.device('cuda', idx))
+            _OWN_STREAMS[idx] = s
+    return s
 
 
 def make_spec(dim, wrap_shape, mesh_shape, conf_cell_size, offset=0, cell_size=None, drop=True):

@@ -288,6 +288,26 @@ extern "C" int pmx_device_sms(int *sms) {
     return PMX_OK;
 }
 
+extern "C" int pmx_stream_create(int device, void **stream) {
+    if (!stream) return fail(PMX_ERR_ARG, "null stream");
+    *stream = nullptr;
+    int prev = 0;
+    PMX_CUDA(cudaGetDevice(&prev));
+    PMX_CUDA(cudaSetDevice(device));
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_status(e, "cudaStreamCreateWithFlags");
+    *stream = reinterpret_cast<void *>(s);
+    return PMX_OK;
+}
+
+extern "C" int pmx_stream_destroy(void *stream) {
+    if (!stream) return PMX_OK;
+    PMX_CUDA(cudaStreamDestroy(reinterpret_cast<cudaStream_t>(stream)));
+    return PMX_OK;
+}
+
 static int check_common(const pmx_enmesh_spec *spec, const void *pmid, const void *disp,
                         int64_t n, EmParams *p) {
     int st = make_em_params(spec, p);

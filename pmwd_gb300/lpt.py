@@ -8,7 +8,7 @@ from itertools import combinations, permutations
 
 import torch
 
-from . import _hostmath
+from . import _hostmath, _lib
 from .boltzmann import growth
 from .cosmology import E2
 from .gravity import laplace, neg_grad
@@ -172,18 +172,22 @@ class _LptGraph:
                 for _ in range(2):   # plans and allocator pools before capture
                     _lpt_device(self.modes, self.fac, self.kvec, self.disp0, self.vel0, conf)
             self.stream.synchronize()
-            # captured on this stream with stream-level syncs only (no device
-            # synchronize, which fails while another thread captures), in
-            # thread-local mode so other threads keep launching meanwhile
+            # captured with stream-level syncs only (no device synchronize,
+            # which fails while another thread captures), in thread-local
+            # mode so other threads keep launching meanwhile, and on a stream
+            # of the library's own: a pooled torch stream may be the stream
+            # another thread launches a request's work on, which the capture
+            # would then record instead of running
+            cap = _lib.own_stream(dev)
             self.graph = torch.cuda.CUDAGraph()
-            with torch.cuda.stream(self.stream):
+            with torch.cuda.stream(cap):
                 self.graph.capture_begin(capture_error_mode='thread_local')
                 try:
                     self.disp, self.vel = _lpt_device(self.modes, self.fac, self.kvec,
                                                       self.disp0, self.vel0, conf)
                 finally:
                     self.graph.capture_end()
-            self.stream.synchronize()
+            cap.synchronize()
 
     def run(self, modes, fac):
         cur = torch.cuda.current_stream(self.dev)

@@ -195,6 +195,54 @@ def test_lpt_graph_concurrent_callers(cuda):
             assert rel_l2(g[1], e.vel.detach().cpu().numpy()) < 1e-6
 
 
+def test_lpt_graph_capture_leaves_pooled_streams_alone(cuda):
+    """torch.cuda.Stream() draws from a fixed pool (32 per device), so a
+    graph captured on a pooled stream would also record the work another
+    thread launches on that same stream (the server's request and group
+    streams are pooled streams).  The 2LPT graphs are captured on a stream
+    the library created: work launched on every pooled stream while a graph
+    is being built runs, and its events can be queried."""
+    import importlib
+    import threading
+    from pmwd_gb300 import _lib
+    glpt = importlib.import_module('pmwd_gb300.lpt')
+    glpt._GRAPHS.clear()
+    streams = [torch.cuda.Stream(device=cuda) for _ in range(64)]
+    pooled = {s.cuda_stream for s in streams}
+    assert len(pooled) < len(streams)                 # the pool wraps around
+    assert _lib.own_stream(cuda).cuda_stream not in pooled
+    conf = pg.Configuration(2.0, (32, 32, 32), 2)
+    cosmo = pg.boltzmann(pg.SimpleLCDM(conf), conf)
+    modes = pg.linear_modes(pg.white_noise(3, conf, device=cuda), cosmo, conf)
+    counts = torch.zeros(len(streams), device=cuda)
+    torch.cuda.synchronize()
+    done = threading.Event()
+
+    def build():
+        try:
+            with torch.no_grad():
+                pg.lpt(modes, cosmo, conf)
+        finally:
+            done.set()
+
+    th = threading.Thread(target=build)
+    th.start()
+    rounds = 0
+    try:
+        while not done.is_set() or rounds < 3:
+            for i, s in enumerate(streams):
+                with torch.cuda.stream(s):
+                    counts[i:i + 1].add_(1.0)
+                    ev = torch.cuda.Event()
+                    ev.record(s)
+                ev.query()
+            rounds += 1
+    finally:
+        th.join()
+    torch.cuda.synchronize()
+    assert torch.all(counts == rounds), counts
+
+
 def test_lpt_statistics_match_published(cuda):
     """docs/examples/quickstart.ipynb prints, for 256^3 particles, spacing 1,
     2x mesh, SimpleLCDM, after 2LPT at a=1/64: disp.std() = 0.105 and
