@@ -13,7 +13,7 @@
 //   g     3 * M       real acceleration meshes (planar, one per axis)
 //   mcot  3 * M       cotangents of g (adjoint workspaces only)
 //   ktab  2*(n0+n1+n2h) angular wavenumbers, plain and Nyquist-masked
-//   part  4 * PMAX    float64 per-block partial sums of the dot products
+//   part  4 * pstride float64 per-block partial sums of the dot products
 // with M = n0*n1*n2 and Mc = n0*n1*(n2/2+1).
 
 #include <cuda.h>
@@ -33,7 +33,13 @@ using namespace pmx;
 
 namespace {
 
-constexpr int PMAX = 65536;      // max blocks of a particle kernel (partials per slot)
+constexpr int PMAX = 4096;       // max blocks of the stand-alone dot kernels (partials)
+// Per-block partial sums per dot slot of a workspace: one per block of a
+// particle kernel, whose grids reach one particle per thread up to 2^27
+// particles (512^3) in a single-simulation workspace; 2^16 per simulation
+// of a batched one.
+constexpr int64_t PART_ONE = int64_t(1) << 19;
+constexpr int64_t PART_SLOT = int64_t(1) << 16;
 constexpr int BMAX = 16;         // most simulations of one batched call
 constexpr int NSLOT = 4;         // dot-product slots
 constexpr int PT = 256;          // threads per particle kernel
@@ -92,6 +98,8 @@ struct pmx_workspace {
     // simulations one call can carry (batched workspaces): every mesh
     // buffer below holds `slots` consecutive copies, slot-major
     int slots = 1;
+    // per-block partial sums per dot slot (and per simulation slot) in part
+    int64_t pstride = 0;
     float *dens = nullptr;
     float2 *ck = nullptr;
     float *g = nullptr;
@@ -329,6 +337,8 @@ struct Hot {
     bool vec;
     // warp-aggregated deposits (mesh indices below 2^32 - 32)
     bool agg;
+    // per-block partial sums: slot s of block b at part[s * pstride + b]
+    int64_t pstride;
 };
 
 __device__ __forceinline__ void hot_axis(const Hot &h, int a, int pm, float d, Axis &ax) {
@@ -891,8 +901,8 @@ __device__ __forceinline__ void ka_body(Hot h, const int16_t *__restrict__ pmid,
         double t0 = block_sum<PT>(s0, sh);
         double t1 = block_sum<PT>(s1, sh);
         if (threadIdx.x == 0) {
-            part[0 * PMAX + blockIdx.x] = t0;
-            part[1 * PMAX + blockIdx.x] = t1;
+            part[0 * h.pstride + blockIdx.x] = t0;
+            part[1 * h.pstride + blockIdx.x] = t1;
         }
     }
 }
@@ -998,7 +1008,7 @@ __device__ __forceinline__ void g3adj_body(Hot h, const int16_t *__restrict__ pm
         __syncwarp();
     }
     double t2 = block_sum<PT>(s2, sh);
-    if (threadIdx.x == 0) part[2 * PMAX + blockIdx.x] = t2;
+    if (threadIdx.x == 0) part[2 * h.pstride + blockIdx.x] = t2;
 }
 
 template <bool WIN, bool AGG = false>
@@ -1208,8 +1218,8 @@ __device__ __forceinline__ void sa_ka_body(Hot h, const int16_t *__restrict__ pm
     double t0 = block_sum<PT>(s0, sh);
     double t1 = block_sum<PT>(s1, sh);
     if (threadIdx.x == 0) {
-        part[0 * PMAX + blockIdx.x] = t0;
-        part[1 * PMAX + blockIdx.x] = t1;
+        part[0 * h.pstride + blockIdx.x] = t0;
+        part[1 * h.pstride + blockIdx.x] = t1;
     }
 }
 
@@ -1228,17 +1238,26 @@ __global__ void __launch_bounds__(PT) k_sa_ka(Hot h, const int16_t *__restrict__
 // Sums the per-block partials in a fixed order: dots[s] = sum of slot s for
 // s < nslots (dots may be NULL), and *om_out = om_scale * sum of slot 2
 // (om_out may be NULL).  Slot 2 holds nblk2 partials (the gather VJP's
-// grid), the other slots nblk.
-__global__ void k_finish(const double *part, int nblk, int nblk2, double *dots, int nslots,
-                         double *om_out, double om_scale) {
+// grid), the other slots nblk; slot s starts at part + s * pstride.
+__global__ void k_finish(const double *part, int64_t pstride, int nblk, int nblk2, double *dots,
+                         int nslots, double *om_out, double om_scale) {
     __shared__ double sh[32];
     int last = nslots > 3 ? nslots : 3;
     for (int s = 0; s < last; ++s) {
         bool want = (dots && s < nslots) || (om_out && s == 2);
         if (!want) continue;
         const int nb = s == 2 ? nblk2 : nblk;
-        double v = 0.0;
-        for (int b = threadIdx.x; b < nb; b += blockDim.x) v += part[s * PMAX + b];
+        const double *p = part + s * pstride;
+        // eight independent partial sums per thread (a fixed order), so the
+        // loads of a large grid's partials overlap
+        double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        int b = threadIdx.x;
+        for (; b + 7 * 1024 < nb; b += 8 * 1024) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] += p[b + u * 1024];
+        }
+        for (; b < nb; b += 1024) a[0] += p[b];
+        double v = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
         double t = block_sum<1024>(v, sh);
         if (threadIdx.x == 0) {
             if (dots && s < nslots) dots[s] = t;
@@ -1310,7 +1329,7 @@ __global__ void __launch_bounds__(PT) k_ka_b(Hot h, const __grid_constant__ Batc
     const SimB &sb = t.s[blockIdx.y];
     ka_body<KD, false, false, AGG>(sim_hot(h, sb), sb.pmid, sb.disp, sb.vel, sb.acc, sb.dcot, sb.vcot,
                               sb.alpha, sb.n, sb.f[0], sb.f[1], slot_ptr(dens, M),
-                              slot_ptr(part, (int64_t)NSLOT * PMAX));
+                              slot_ptr(part, NSLOT * h.pstride));
 }
 
 // acc_cot: the simulation's vel_cot (steps) or the given cotangent of acc
@@ -1322,7 +1341,7 @@ __global__ void __launch_bounds__(PT) k_g3adj_b(Hot h, const __grid_constant__ B
     const SimB &sb = t.s[blockIdx.y];
     g3adj_body<false, AGG>(sim_hot(h, sb), sb.pmid, sb.disp, sb.vcot, sb.acc, sb.alpha, sb.n, M,
                       slot_ptr(g, 3 * M), slot_ptr(mcot, 3 * M),
-                      slot_ptr(part, (int64_t)NSLOT * PMAX));
+                      slot_ptr(part, NSLOT * h.pstride));
 }
 
 template <bool KICK>
@@ -1340,7 +1359,7 @@ __global__ void __launch_bounds__(PT) k_sa_ka_b(Hot h, const __grid_constant__ B
     const SimB &sb = t.s[blockIdx.y];
     sa_ka_body<AGG>(sim_hot(h, sb), sb.pmid, sb.disp, sb.vel, sb.acc, sb.dcot, sb.vcot, sb.alpha, sb.n,
                slot_ptr(rcot, M), sb.f[0], sb.f[1], sb.f[2], slot_ptr(dens, M),
-               slot_ptr(part, (int64_t)NSLOT * PMAX));
+               slot_ptr(part, NSLOT * h.pstride));
 }
 
 // k_finish of every simulation of a batch (block b: slot b): dots[b][0..3)
@@ -1349,15 +1368,15 @@ struct FinishTab {
     double *dots[BMAX];
     double oms[BMAX];
 };
-__global__ void k_finish_b(const double *part, int nblk, const __grid_constant__ FinishTab t,
-                           int ndots) {
+__global__ void k_finish_b(const double *part, int64_t pstride, int nblk,
+                           const __grid_constant__ FinishTab t, int ndots) {
     __shared__ double sh[32];
-    const double *pp = part + blockIdx.x * (int64_t)NSLOT * PMAX;
+    const double *pp = part + blockIdx.x * NSLOT * pstride;
     double *dots = t.dots[blockIdx.x];
     for (int s = 0; s < 3; ++s) {
         if (s >= ndots && s != 2) continue;
         double v = 0.0;
-        for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += pp[s * PMAX + b];
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += pp[s * pstride + b];
         double tt = block_sum<1024>(v, sh);
         if (threadIdx.x == 0) {
             if (s < ndots) dots[s] = tt;
@@ -1438,22 +1457,25 @@ namespace {
 
 int grid_fill(int64_t n) { return stride_grid((n + 3) / 4, 256, 16); }
 
-// Blocks of a grid-stride particle kernel: up to per_sm per SM, at most
-// PMAX.  Many short blocks beat a few long-running ones.  The block
-// scheduler starts a new block whenever one ends, so warps slowed by
-// contended atomics (the halos of late, clustered steps) hold up only their
-// own block and not a fixed share of the particles.  Measured on a
-// 512^3-particle / 1024^3-mesh run: a 100 + 100 step forward and adjoint
-// run takes 120 ms per step pair at 65536 blocks, 130 at 64 per SM, 140 at
-// 8 per SM; the early steps 90.9 / 91.4 / 93.8 ms; one resident wave of
-// blocks was slower still.
-int ptcl_grid(int64_t n, int per_sm = PMAX) {
-    const int g = stride_grid(n, PT, per_sm);
-    return g > PMAX ? PMAX : g;
+// Blocks of a grid-stride particle kernel: one particle per thread, or at
+// most per_sm blocks per SM, and never more than the workspace holds
+// partial sums for.  Many short blocks beat a few long-running ones: the
+// block scheduler starts a new block whenever one ends, so warps slowed by
+// contended atomics (the halos of the late, clustered steps) hold up only
+// their own block, not a fixed share of the particles.  Measured on the
+// 512^3-particle / 1024^3-mesh run, ms per forward + adjoint step pair over
+// all 100 + 100 steps (over the first 10 + 10): one particle per thread
+// 112.8 (90.1); 65536 blocks 121.3 (90.7); 64 blocks per SM 130 (91.4); 8
+// per SM 140 (93.8); one resident wave of blocks slower still.
+int ptcl_grid(const pmx_workspace *ws, int64_t n, int per_sm = 1 << 30) {
+    const int64_t g = stride_grid(n, PT, per_sm);
+    return (int)(g < ws->pstride ? g : ws->pstride);
 }
-// The joined scatter-VJP / adjoint-kick pass measured best at 64 blocks per
-// SM (5.59 vs 5.84 ms per launch at 65536 blocks).
-constexpr int SAKA_PER_SM = 64;
+// The kernels that also sum two dot products per block (the adjoint's
+// kick/drift passes) measured best at 64 blocks per SM: k_sa_ka 5.59 ms per
+// launch vs 5.84 at 65536 blocks, k_ka 0.56 vs 0.80 ms at one particle per
+// thread.
+constexpr int DOT2_PER_SM = 64;
 
 // Per-device reduction scratch for the stand-alone dot entry points,
 // allocated once at their first use on a device.
@@ -1520,6 +1542,7 @@ int check_hot(pmx_workspace *ws, const pmx_enmesh_spec *spec, const void *pmid, 
     // more than the scalar atomics they replace): opt-in, PMX_WS_VEC
     h->vec = ws->vec;
     h->agg = ws->agg;
+    h->pstride = ws->pstride;
     if (ws->xfast) {
         h->gxs = 2 * ws->n1 * ws->n2;
         h->gjs = ws->n1 * ws->n2;
@@ -1837,7 +1860,7 @@ size_t buffers_bytes(const int64_t s[3], int32_t flags, int32_t slots) {
     int64_t M = s[0] * s[1] * s[2], Mc = s[0] * s[1] * (s[2] / 2 + 1);
     size_t b = (size_t)M * 4 + (size_t)Mc * 8 * 3 + (size_t)M * 4 * 3;
     if (flags & PMX_WS_ADJOINT) b += (size_t)M * 4 * 3;
-    b += (size_t)NSLOT * PMAX * 8;
+    b += (size_t)NSLOT * (slots == 1 ? PART_ONE : PART_SLOT) * 8;
     return b * (size_t)slots + (size_t)2 * (s[0] + s[1] + s[2] / 2 + 1) * 4;
 }
 
@@ -1908,6 +1931,7 @@ static int ws_create(const int64_t mesh_shape[3], int32_t flags, int32_t slots,
     pmx_workspace *ws = new pmx_workspace();
     ws->flags = flags;
     ws->slots = slots;
+    ws->pstride = slots == 1 ? PART_ONE : PART_SLOT;
     ws->n0 = mesh_shape[0];
     ws->n1 = mesh_shape[1];
     ws->n2 = mesh_shape[2];
@@ -1937,7 +1961,7 @@ static int ws_create(const int64_t mesh_shape[3], int32_t flags, int32_t slots,
     if ((st = alloc((void **)&ws->dens, B * ws->M * 4)) ||
         (st = alloc((void **)&ws->ck, B * ws->n0 * ws->n1 * ws->n2p * 8 * 3)) ||
         (st = alloc((void **)&ws->g, B * ws->M * 4 * 3)) || (st = alloc((void **)&ws->ktab, ktn * 4)) ||
-        (st = alloc((void **)&ws->part, B * NSLOT * PMAX * 8)) ||
+        (st = alloc((void **)&ws->part, B * NSLOT * ws->pstride * 8)) ||
         ((flags & PMX_WS_ADJOINT) && (st = alloc((void **)&ws->mcot, B * ws->M * 4 * 3)))) {
         ws_free(ws);
         return st;
@@ -2099,7 +2123,7 @@ extern "C" int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec, const i
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
-            PMX_WIN_LAUNCH(h, k_kds, (false), ptcl_grid(n), WIN1_SMEM, s,
+            PMX_WIN_LAUNCH(h, k_kds, (false), ptcl_grid(ws, n), WIN1_SMEM, s,
                            (h, pmid, const_cast<float *>(disp), nullptr, nullptr, n, 0.f, 0.f,
                             ws->dens));
             PMX_LAUNCH_CHECK("k_kds");
@@ -2110,10 +2134,10 @@ extern "C" int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec, const i
         {
             Stage sg(ws, 5, s, 1);
             if (ws->tma)
-                k_gather3_tma<false><<<ptcl_grid(n), PT, TMA_SMEM, s>>>(
+                k_gather3_tma<false><<<ptcl_grid(ws, n), PT, TMA_SMEM, s>>>(
                     h, ws->tmap, pmid, disp, nullptr, acc, n, ws->g, 0.f, ws->err);
             else
-            k_gather3<false, false><<<ptcl_grid(n), PT, 0, s>>>(h, pmid, disp, nullptr, acc, n,
+            k_gather3<false, false><<<ptcl_grid(ws, n), PT, 0, s>>>(h, pmid, disp, nullptr, acc, n,
                                                                 ws->M, ws->g, 0.f);
             PMX_LAUNCH_CHECK("k_gather3");
         }
@@ -2138,7 +2162,7 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
         k_fill<<<grid_fill(3 * ws->M), 256, 0, s>>>(ws->mcot, 0.f, 3 * ws->M);
         PMX_LAUNCH_CHECK("k_fill");
     }
-    const int G = ptcl_grid(n);
+    const int G = ptcl_grid(ws, n);
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
@@ -2179,7 +2203,7 @@ extern "C" int pmx_force_vjp(pmx_workspace *ws, const pmx_enmesh_spec *spec, con
         } else {
             {
                 Stage sg(ws, 12, s, 1);
-                k_finish<<<1, 1024, 0, s>>>(ws->part, G, G, nullptr, 0, omega_m_cot,
+                k_finish<<<1, 1024, 0, s>>>(ws->part, ws->pstride, G, G, nullptr, 0, omega_m_cot,
                                             om_scale(omega_m));
                 PMX_LAUNCH_CHECK("k_finish");
             }
@@ -2295,7 +2319,7 @@ static int nbody_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int1
         k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
         PMX_LAUNCH_CHECK("k_fill");
     }
-    const int G = ptcl_grid(n);
+    const int G = ptcl_grid(ws, n);
     if (n > 0) {
         {
             Stage sg(ws, 1, s, 1);
@@ -2349,10 +2373,10 @@ static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const 
         PMX_CUDA(cudaMemsetAsync(dots, 0, 4 * sizeof(double), s));
         return PMX_OK;
     }
-    const int G = ptcl_grid(n);
+    const int G = ptcl_grid(ws, n), G2 = ptcl_grid(ws, n, DOT2_PER_SM);
     {
         Stage sg(ws, 6, s, 1);
-        PMX_WIN_LAUNCH(h, k_ka, (true), G, WIN1_SMEM, s,
+        PMX_WIN_LAUNCH(h, k_ka, (true), G2, WIN1_SMEM, s,
                        (h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot, n, factors[0],
                         factors[1], ws->dens, ws->part));
         PMX_LAUNCH_CHECK("k_ka");
@@ -2384,7 +2408,8 @@ static int nbody_adj_step(pmx_workspace *ws, const pmx_enmesh_spec *spec, const 
     }
     {
         Stage sg(ws, 12, s, 1);
-        k_finish<<<1, 1024, 0, s>>>(ws->part, G, G, dots, 3, dots + 3, om_scale(omega_m));
+        k_finish<<<1, 1024, 0, s>>>(ws->part, ws->pstride, G2, G, dots, 3, dots + 3,
+                                    om_scale(omega_m));
         PMX_LAUNCH_CHECK("k_finish");
     }
     return PMX_OK;
@@ -2452,7 +2477,7 @@ static int nbody_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const int
     }
     cudaStream_t s = as_stream(stream);
     if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
-    const int G = ptcl_grid(n);
+    const int G = ptcl_grid(ws, n);
     {
         Stage sg(ws, 0, s, 1);
         k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
@@ -2521,8 +2546,8 @@ static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const
     }
     cudaStream_t s = as_stream(stream);
     if ((st = ensure_ktab(ws, spec->conf_cell_size, s))) return st;
-    const int G = ptcl_grid(n), Gsaka = ptcl_grid(n, SAKA_PER_SM);
-    int nb01 = G;  // blocks of the kernel that last wrote dot slots 0 and 1
+    const int G = ptcl_grid(ws, n), G2 = ptcl_grid(ws, n, DOT2_PER_SM);
+    int nb01 = G2;  // blocks of the kernel that last wrote dot slots 0 and 1
     {
         Stage sg(ws, 0, s, 2);
         k_fill<<<grid_fill(ws->M), 256, 0, s>>>(ws->dens, -1.f, ws->M);
@@ -2532,13 +2557,13 @@ static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const
     {
         Stage sg(ws, 6, s, 1);
         if (h.agg)
-            k_ka<true, false, false, true><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot,
-                                                            vel_cot, acc_cot, n, factors[0],
-                                                            factors[1], ws->dens, ws->part);
+            k_ka<true, false, false, true><<<G2, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot,
+                                                             vel_cot, acc_cot, n, factors[0],
+                                                             factors[1], ws->dens, ws->part);
         else
-            k_ka<true, false, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot,
-                                                        acc_cot, n, factors[0], factors[1],
-                                                        ws->dens, ws->part);
+            k_ka<true, false, false><<<G2, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot,
+                                                         acc_cot, n, factors[0], factors[1],
+                                                         ws->dens, ws->part);
         PMX_LAUNCH_CHECK("k_ka");
     }
     for (int32_t i = 0; i < nsteps; ++i) {
@@ -2556,7 +2581,8 @@ static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const
         }
         {
             Stage sg(ws, 12, s, 1);
-            k_finish<<<1, 1024, 0, s>>>(ws->part, nb01, G, dots + 4 * i, 3, dots + 4 * i + 3,
+            k_finish<<<1, 1024, 0, s>>>(ws->part, ws->pstride, nb01, G, dots + 4 * i, 3,
+                                        dots + 4 * i + 3,
                                         om_scale(omega_m));
             PMX_LAUNCH_CHECK("k_finish");
         }
@@ -2570,15 +2596,15 @@ static int nbody_adj_steps(pmx_workspace *ws, const pmx_enmesh_spec *spec, const
             }
             Stage sg(ws, 14, s, 1);
             if (h.agg)
-                k_sa_ka<true><<<Gsaka, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot,
+                k_sa_ka<true><<<G2, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot,
                                                    acc_cot, n, ws->rcot_of(1), f[2], f[3], f[4],
                                                    ws->dens, ws->part);
             else
-                k_sa_ka<<<Gsaka, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot,
+                k_sa_ka<<<G2, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, vel_cot, acc_cot,
                                              n, ws->rcot_of(1), f[2], f[3], f[4], ws->dens,
                                              ws->part);
             PMX_LAUNCH_CHECK("k_sa_ka");
-            nb01 = Gsaka;
+            nb01 = G2;
         } else {
             Stage sg(ws, 11, s, 1);
             k_sadj<true, false><<<G, PT, 0, s>>>(h, pmid, disp, vel, acc, disp_cot, acc_cot, n,
@@ -2661,7 +2687,7 @@ int batch_prepare(pmx_workspace *ws, const pmx_enmesh_spec *spec, int32_t nsim,
         bc->fin.oms[b] = om_scale(q.omega_m);
         if (q.n > nmax) nmax = q.n;
     }
-    bc->G = ptcl_grid(nmax);
+    bc->G = ptcl_grid(ws, nmax);
     return PMX_OK;
 }
 
@@ -2760,7 +2786,7 @@ extern "C" int pmx_nbody_adj_steps_batch(pmx_workspace *ws, const pmx_enmesh_spe
         FinishTab ft = bc.fin;
         for (int b = 0; b < bc.nb; ++b) ft.dots[b] = bc.fin.dots[b] + 4 * row;
         Stage sg(ws, 12, s, 1);
-        k_finish_b<<<bc.nb, 1024, 0, s>>>(ws->part, bc.G, ft, ndots);
+        k_finish_b<<<bc.nb, 1024, 0, s>>>(ws->part, ws->pstride, bc.G, ft, ndots);
         PMX_LAUNCH_CHECK("k_finish_b");
         return PMX_OK;
     };

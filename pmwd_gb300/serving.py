@@ -94,12 +94,15 @@ def request_bytes(side, grad):
     return 42 * n + (48 * n if grad else 0) + 64 * n
 
 
-def workspace_bytes(mesh_side):
-    """Meshes and spectra of one workspace slot plus a cuFFT work-area
-    allowance and the per-block float64 partial sums (4 x 65536)."""
+def workspace_bytes(mesh_side, slots=1):
+    """Meshes and spectra of a workspace with `slots` simulation slots, a
+    cuFFT work-area allowance, and the per-block float64 partial sums of the
+    particle kernels (4 x 2^19 in a single-simulation workspace, 4 x 2^16 per
+    slot of a batched one)."""
     m = mesh_side ** 3
     mc = mesh_side * mesh_side * (mesh_side // 2 + 1)
-    return 4 * m + 3 * 8 * mc + 6 * 4 * m + 8 * mc + 4 * 65536 * 8
+    part = 4 * 8 * (2 ** 19 if slots == 1 else slots * 2 ** 16)
+    return slots * (4 * m + 3 * 8 * mc + 6 * 4 * m + 8 * mc) + part
 
 
 def batchable(mesh_side):
@@ -113,7 +116,8 @@ def group_slots(mesh_side, budget):
     apply."""
     if not batchable(mesh_side):
         return 1
-    return int(max(1, min(MAX_SLOTS, (0.25 * budget) // workspace_bytes(mesh_side))))
+    per_slot = workspace_bytes(mesh_side, MAX_SLOTS) / MAX_SLOTS
+    return int(max(1, min(MAX_SLOTS, (0.25 * budget) // per_slot)))
 
 
 class Job:
@@ -385,7 +389,7 @@ class GpuEngine:
 
     def group_bytes(self, key):
         s = self.slots(key)
-        return s * workspace_bytes(key[0]) if s > 1 else 0
+        return workspace_bytes(key[0], s) if s > 1 else 0
 
     def job_bytes(self, req):
         key = (req.ptcl_side * req.mesh_factor, req.ptcl_spacing / req.mesh_factor)
