@@ -251,3 +251,15 @@ def test_results_same_alone_and_in_one_batched_group(cuda):
         if a.grad_rms is not None:
             assert abs(m.grad_rms / a.grad_rms - 1) < 5e-3
             assert abs(m.dobj_dOm / a.dobj_dOm - 1) < 5e-3
+
+
+def test_workspace_bytes_counts_the_partials():
+    """A workspace's estimate counts its meshes per slot plus the particle
+    kernels' per-block float64 partial sums: 4 x 2^19 in a single-simulation
+    workspace (one per block at one particle per thread), 4 x 2^16 per slot
+    of a batched one."""
+    one, two, eight = (serving.workspace_bytes(256, s) for s in (1, 2, 8))
+    mesh = (two - 2 * 4 * 8 * 2 ** 16) / 2
+    assert one == mesh + 4 * 8 * 2 ** 19
+    assert eight == 8 * mesh + 8 * 4 * 8 * 2 ** 16
+    assert mesh > 30 * 256 ** 3            # meshes, spectra and work areas
