@@ -178,26 +178,27 @@ def stream_ptr(device=None):
     return c_p(torch.cuda.current_stream(device).cuda_stream)
 
 
-_OWN_STREAMS = {}
-_OWN_LOCK = threading.Lock()
+_LIB_STREAMS = {}
+_LIB_STREAM_LOCK = threading.Lock()
 
 
-def own_stream(device):
-    """A CUDA stream the library created on ``device`` (one per device, kept
-    for the life of the process), as a ``torch.cuda.ExternalStream``.
-    ``torch.cuda.Stream()`` hands out streams from a fixed pool (32 per
-    device), so a pooled stream may be the one another thread launches its
-    work on; graph captures use this stream instead, so that a capture
-    never records another thread's work."""
+def lib_stream(device):
+    """A non-blocking CUDA stream that the library created on ``device``
+    (``pmx_stream_create``; one per device, kept for the life of the
+    process), as a ``torch.cuda.ExternalStream``.  ``torch.cuda.Stream()``
+    hands out streams from a fixed pool (32 per device), so a pooled stream
+    may be the very stream another thread launches its work on, and a graph
+    captured on it would record that work too; this stream is never handed
+    to anyone else."""
     dev = torch.device(device)
     idx = dev.index if dev.index is not None else torch.cuda.current_device()
-    with _OWN_LOCK:
-        s = _OWN_STREAMS.get(idx)
+    with _LIB_STREAM_LOCK:
+        s = _LIB_STREAMS.get(idx)
         if s is None:
             h = c_p()
             check(load().pmx_stream_create(idx, ctypes.byref(h)), 'pmx_stream_create')
             s = torch.cuda.ExternalStream(h.value, device=torch.device('cuda', idx))
-            _OWN_STREAMS[idx] = s
+            _LIB_STREAMS[idx] = s
     return s
 
 

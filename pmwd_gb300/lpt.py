@@ -140,8 +140,9 @@ def _lpt_device(modes, fac, kvec, disp0, vel0, conf):
 # grids, where launching ~10^3 small kernels one by one would cost more than
 # the transforms themselves.  One graph per (configuration, device); the
 # growth factors are a graph input, so a graph serves every cosmology.
-# Replays run on the graph's own stream under a lock, so concurrent callers
-# (the serving threads) never share the static buffers in flight.
+# Builds and replays run on one library-created stream per device under a
+# lock, so concurrent callers (the serving threads) never share the static
+# buffers in flight and no replay lands in another graph's capture.
 GRAPH_MAX_PTCL = 256 ** 3
 _GRAPHS = OrderedDict()
 _GRAPHS_MAX = 8
@@ -151,7 +152,12 @@ _GRAPH_LOCK = threading.Lock()
 class _LptGraph:
     def __init__(self, conf, dev, spec_shape):
         self.conf, self.dev = conf, dev
-        self.stream = torch.cuda.Stream(dev)
+        # warm-up, capture and every replay on the library's own stream (one
+        # per device, shared by the graphs; built with the replay lock held,
+        # so no replay is enqueued on it during a capture): a pooled torch
+        # stream may be the stream another thread launches a request's work
+        # on, which a capture would then record as well
+        self.stream = _lib.lib_stream(dev)
         self.modes = torch.zeros(spec_shape, dtype=torch.complex64, device=dev)
         self.fac = torch.zeros((conf.lpt_order, 2), dtype=torch.float32, device=dev)
         # pinned staging for the factors: a ring, each slot reused only after
@@ -172,22 +178,18 @@ class _LptGraph:
                 for _ in range(2):   # plans and allocator pools before capture
                     _lpt_device(self.modes, self.fac, self.kvec, self.disp0, self.vel0, conf)
             self.stream.synchronize()
-            # captured with stream-level syncs only (no device synchronize,
-            # which fails while another thread captures), in thread-local
-            # mode so other threads keep launching meanwhile, and on a stream
-            # of the library's own: a pooled torch stream may be the stream
-            # another thread launches a request's work on, which the capture
-            # would then record instead of running
-            cap = _lib.own_stream(dev)
+            # captured on this stream with stream-level syncs only (no device
+            # synchronize, which fails while another thread captures), in
+            # thread-local mode so other threads keep launching meanwhile
             self.graph = torch.cuda.CUDAGraph()
-            with torch.cuda.stream(cap):
+            with torch.cuda.stream(self.stream):
                 self.graph.capture_begin(capture_error_mode='thread_local')
                 try:
                     self.disp, self.vel = _lpt_device(self.modes, self.fac, self.kvec,
                                                       self.disp0, self.vel0, conf)
                 finally:
                     self.graph.capture_end()
-            cap.synchronize()
+            self.stream.synchronize()
 
     def run(self, modes, fac):
         cur = torch.cuda.current_stream(self.dev)
@@ -224,11 +226,10 @@ def _graph_for(conf, modes):
             _GRAPHS.move_to_end(key)
             return g
     with _BUILD_LOCK:   # one capture at a time; a racing caller finds it built
-        with _GRAPH_LOCK:
+        with _GRAPH_LOCK:   # and no replay on the shared stream meanwhile
             g = _GRAPHS.get(key)
-        if g is None:
-            g = _LptGraph(conf, modes.device, tuple(modes.shape))
-            with _GRAPH_LOCK:
+            if g is None:
+                g = _LptGraph(conf, modes.device, tuple(modes.shape))
                 _GRAPHS[key] = g
                 while len(_GRAPHS) > _GRAPHS_MAX:
                     _GRAPHS.popitem(last=False)
