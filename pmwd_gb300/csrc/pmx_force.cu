@@ -1248,8 +1248,8 @@ __global__ void k_finish(const double *part, int64_t pstride, int nblk, int nblk
         if (!want) continue;
         const int nb = s == 2 ? nblk2 : nblk;
         const double *p = part + s * pstride;
-        // eight independent partial sums per thread (a fixed order), so the
-        // loads of a large grid's partials overlap
+        // eight independent partial sums per thread of the 1024 (a fixed
+        // order), so the loads of a large grid's partials overlap
         double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         int b = threadIdx.x;
         for (; b + 7 * 1024 < nb; b += 8 * 1024) {
@@ -2137,8 +2137,8 @@ extern "C" int pmx_force(pmx_workspace *ws, const pmx_enmesh_spec *spec, const i
                 k_gather3_tma<false><<<ptcl_grid(ws, n), PT, TMA_SMEM, s>>>(
                     h, ws->tmap, pmid, disp, nullptr, acc, n, ws->g, 0.f, ws->err);
             else
-            k_gather3<false, false><<<ptcl_grid(ws, n), PT, 0, s>>>(h, pmid, disp, nullptr, acc, n,
-                                                                ws->M, ws->g, 0.f);
+                k_gather3<false, false><<<ptcl_grid(ws, n), PT, 0, s>>>(h, pmid, disp, nullptr,
+                                                                    acc, n, ws->M, ws->g, 0.f);
             PMX_LAUNCH_CHECK("k_gather3");
         }
     }
