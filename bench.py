@@ -567,8 +567,9 @@ def run_pmx(args, rank, world, local_rank):
                 'frac': ach / peak, 'traffic': tr,
                 'algorithmic_bytes': ab[dom], 'peak_kind': f'{peak_kind} (MEASURED_PEAKS.json hbm_gbs)'
                 if peak_kind == 'measured' else 'fallback 6.8 TB/s'}
-    # whole-step compulsory bytes, the fixed convention of the hot-path
-    # survey: forward step 156 N + 64 M, adjoint step 336 N + 140 M
+    # whole-step compulsory bytes, a fixed convention (each stage's
+    # compulsory operands once): forward step 156 N + 64 M, adjoint step
+    # 336 N + 140 M
     step_bytes = 492 * N + 204 * M
     step_gbs = step_bytes / (ms_step / 1e3) / 1e9
 

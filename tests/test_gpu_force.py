@@ -191,7 +191,7 @@ def test_nbody_forward_matches_oracle(cuda, nb_case):
     oconf, gconf, pmid, disp, vel, ocos, gcos = nb_case
     st = onb.nbody(onb.State(pmid, disp, vel), ocos, oconf)
     out = _run_gpu_nbody(gconf, pmid, disp, vel, gcos, cuda)
-    # position RMS within 1e-3 of the particle spacing (spec tier 3)
+    # position RMS within 1e-3 of the particle spacing (the stated full-run bar)
     rms = np.sqrt(np.mean((out.disp.cpu().numpy().astype(np.float64) - st.disp) ** 2))
     assert rms < 1e-3 * oconf.ptcl_spacing
     assert rel_l2(out.disp.cpu().numpy(), st.disp) < 1e-4

@@ -14,7 +14,7 @@ from pmwd_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
 
-RTOL_MESH = 1e-5      # density-mesh relative L2 of a single scatter (spec tier 2)
+RTOL_MESH = 1e-5      # density-mesh relative L2 of a single scatter (the stated bar)
 
 
 def rel_l2(a, b):
